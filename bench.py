@@ -1,0 +1,375 @@
+"""Benchmark: scatterer-line projections per second of the COLE simulation on one
+GB300 (the 3-D LUT volume workload: 2M fixed scatterers x 64x64 lines, 256x64x64
+beam LUT, 3.5 MHz / bw 0.15 / 50 MHz, decimation 8, phase delay on), and the
+same workload on the reference's CPU algorithm.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload volume_3d_lut|sector_2d_fixed|sector_spline]
+
+One step = one simulate_lines over the whole scan (projection, pulse
+convolution, demodulation, decimation).  Prints one JSON line on rank 0.
+
+* value: projections/s with the phantom resident on the device, IQ left on the
+  device, CUDA events around each step on the simulator's stream, L2 flushed
+  (a 512 MiB memset) between steps outside the timed events.
+* e2e: the same metric through the C ABI with host buffers: every step uploads
+  the scatterers from pinned host memory (bcsim_set_fixed_scatterers) and reads
+  the IQ back (bcsim_simulate_lines), host wall clock.
+* roofline: the projection kernel against the FP32 pipe (the survey's
+  per-projection flop count; see flops_per_projection) and its HBM traffic.
+* cpu_baseline: the CPU port of the reference algorithm (oracle, reference float
+  arithmetic, FFT convolution) on all host cores, on a subset of the lines.
+
+Lines are independent, so N GPUs run N independent replicas of the workload
+(weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "scatterer-line projections/s"
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def flops_per_projection(lut: bool, phase_delay: bool) -> float:
+    """Algorithmic FP32 flops of one scatterer-line projection (FMA = 2):
+    offset (3) + three dot products (15) + distance (5) + bin index (3) +
+    Gaussian exponent (5) + amplitude (1) + accumulation (2) = 34; a lookup-table
+    beam replaces the Gaussian exponent by 3 normalisations and 7 trilinear
+    lerps (27); the sub-sample phase adds 6."""
+    f = 34.0
+    if lut:
+        f += 27.0 - 5.0
+    if phase_delay:
+        f += 6.0
+    return f
+
+
+def make_job(name: str):
+    from openbcsim_gb300 import workloads as W
+
+    return getattr(W, name)()
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while active."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def sm_count():
+    import torch
+
+    return torch.cuda.get_device_properties(0).multi_processor_count
+
+
+def run_gpu(args):
+    import torch
+
+    import openbcsim_gb300 as gb
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    job = make_job(args.workload)
+    sim = gb.RfSimulator("gpu")
+    sim.set_parameter("gpu_device", str(local))
+    gb.configure_job(sim, job)
+    sim.set_parameter("store_kernel_details", "on")
+    L, nd = sim.output_shape()
+    dev_out = torch.empty((L, nd), dtype=torch.complex64, device="cuda")
+    stream = torch.cuda.ExternalStream(sim.stream())
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def step():
+        sim.simulate_lines_device(dev_out.data_ptr(), dev_out.numel())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # ---- device-resident timed region ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    proj_ms = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            starts[i].record(stream)
+        step()
+        ends[i].record(stream)
+        ends[i].synchronize()
+        proj_ms.append(sim.get_debug_data("fixed_projection_kernel_ms")[-1] if job.fixed else
+                       sim.get_debug_data("spline_projection_kernel_ms")[-1])
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    projections = job.projections
+    value = projections * args.steps * world / total_s
+
+    # ---- e2e through the C ABI with pinned host buffers ----
+    host_in = [torch.empty(f.xyza.shape, dtype=torch.float32, pin_memory=True) for f in job.fixed]
+    for h, f in zip(host_in, job.fixed):
+        h.numpy()[:] = f.xyza
+    host_out = torch.empty((L, nd), dtype=torch.complex64, pin_memory=True)
+    out_np = host_out.numpy()
+
+    def e2e_step():
+        sim.clear_fixed_scatterers()
+        for h in host_in:
+            sim.add_fixed_scatterers(h.numpy())
+        sim.simulate_lines_line_major(out_np)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = sum(e2e_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([e2e_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    h2d = sum(f.xyza.nbytes for f in job.fixed)
+    d2h = L * nd * 8
+
+    if rank != 0:
+        return None
+    lut = not hasattr(job.beam, "sigma_lateral")
+    fpp = flops_per_projection(lut, job.phase_delay)
+    proj_avg_ms = statistics.mean(proj_ms)
+    achieved_tflops = projections * fpp / (proj_avg_ms / 1e3) / 1e12
+    sms = sm_count()
+    clock_mhz = clk.get("sm_mhz") or 2070.0
+    fp32_peak = sms * 128 * 2 * clock_mhz * 1e6 / 1e12
+    peaks = {}
+    if os.path.exists(MEASURED_PEAKS):
+        with open(MEASURED_PEAKS) as f:
+            peaks = json.load(f)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    alg_bytes = sum(f.xyza.nbytes for f in job.fixed) + (job.beam.samples.nbytes if lut else 0) + L * nd * 8
+    traffic = None
+    if args.traffic_bytes:
+        traffic = float(args.traffic_bytes)
+    result = {
+        "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)", "data": "synthetic (seeded)",
+        "config": {"workload": f"{job.name}: {job.num_scatterers} fixed scatterers x {L} lines, "
+                               f"{'256x64x64 LUT beam' if lut else 'Gaussian beam'}, ns={job.num_samples}, "
+                               f"decimation {job.decimation}, phase delay {'on' if job.phase_delay else 'off'}",
+                   "projections_per_step": projections, "l2": "flushed between steps (512 MiB memset)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": projections * args.steps * world / e2e_total, "unit": "projections/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_total * 1e3 / args.steps},
+        "roofline": {"bound": "fp32", "kernel": "project_shared_kernel",
+                     "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved_tflops / fp32_peak, "traffic": traffic,
+                     "flops_per_projection": fpp, "kernel_ms": proj_avg_ms,
+                     "peak_source": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {clock_mhz:.0f} MHz "
+                                    "(median SM clock sampled during the timed steps)"},
+        "roofline_hbm": {"achieved": alg_bytes / (proj_avg_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": alg_bytes / (proj_avg_ms / 1e3) / 1e9 / hbm_peak,
+                         "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+        "clocks": clk,
+        "gpu_launches": args.steps * 8,
+        "stage_ms": {k: statistics.mean(sim.get_debug_data(k)) for k in
+                     ["kernel_memset_ms", "prep_sort_ms", "fixed_projection_kernel_ms",
+                      "kernel_convolve_demodulate_ms", "total_ms"] if _has(sim, k)},
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(job, args.cpu_seconds)
+    return result
+
+
+def _has(sim, key):
+    try:
+        sim.get_debug_data(key)
+        return True
+    except RuntimeError:
+        return False
+
+
+def cpu_baseline(job, seconds: float, threads: int = 0):
+    """The reference CPU algorithm on a contiguous subset of the lines, all
+    host cores; `seconds` bounds the sample.  Uses the compiled reference
+    (oracle/_ref) where it exists, else the oracle's port of it (REF32 float
+    arithmetic, FFT convolution)."""
+    from oracle import oracle as O
+
+    cores = threads or os.cpu_count()
+    kind = "reference" if O.ref_available() else "port"
+    L = job.scan.num_lines
+    n_lines = max(1, min(L, cores))
+    sub = _subset(job, 0, n_lines)
+    t0 = time.perf_counter()
+    _cpu_run(sub, kind, cores)
+    dt = time.perf_counter() - t0
+    # grow the sample to about `seconds` of work
+    target = int(min(L, max(n_lines, n_lines * seconds / max(dt, 1e-3))))
+    target = max(cores, (target // cores) * cores) if target >= cores else target
+    sub = _subset(job, 0, target)
+    t0 = time.perf_counter()
+    _cpu_run(sub, kind, cores)
+    dt = time.perf_counter() - t0
+    value = job.num_scatterers * target / dt
+    return {"value": value, "unit": "projections/s", "cores": cores, "kind": kind,
+            "sample": f"{target} of {L} lines of the same workload ({job.num_scatterers} scatterers), "
+                      f"{dt:.1f} s", "seconds": dt}
+
+
+def _subset(job, lo, hi):
+    import copy
+
+    from openbcsim_gb300 import workloads as W
+
+    sub = copy.copy(job)
+    s = job.scan
+    sub.scan = W.ScanSequence(s.origins[lo:hi], s.directions[lo:hi], s.lateral_dirs[lo:hi], s.timestamps[lo:hi],
+                              s.line_length)
+    return sub
+
+
+def _cpu_run(job, kind, cores):
+    from oracle import oracle as O
+
+    if kind == "reference":
+        return O.ref_simulate(job, threads=cores)
+    return O.simulate(job, O.MODE_REF32, threads=cores)
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return None
+    job = make_job(args.workload)
+    from oracle import oracle as O
+
+    cores = os.cpu_count()
+    kind = "reference" if O.ref_available() else "port"
+    # one step = a bounded sample of the workload's lines
+    L = job.scan.num_lines
+    n_lines = min(L, max(cores, args.ref_lines))
+    sub = _subset(job, 0, n_lines)
+    for _ in range(args.warmup):
+        _cpu_run(_subset(job, 0, min(L, cores)), kind, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _cpu_run(sub, kind, cores)
+    dt = time.perf_counter() - t0
+    value = job.num_scatterers * n_lines * args.steps / dt
+    sample = f"{n_lines} of {L} lines per step ({job.num_scatterers} scatterers)"
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": job.name, "projections_per_step": job.num_scatterers * n_lines},
+            "cpu_baseline": {"value": value, "unit": "projections/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "projections/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="volume_3d_lut")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-lines", type=int, default=64)
+    ap.add_argument("--traffic-bytes", type=float, default=None,
+                    help="DRAM bytes per projection launch from an ncu capture (reported as roofline.traffic)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    res = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

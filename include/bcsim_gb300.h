@@ -1,0 +1,147 @@
+/*
+ * bcsim_gb300.h -- C ABI of the GB300 COLE ultrasound line simulator.
+ *
+ * This is the drop-in boundary for the reference's algorithm interface
+ * bcsim::IAlgorithm (src/core/LibBCSim.hpp:42-91) and its factory
+ * bcsim::Create (src/core/LibBCSim.cpp:39-49), flattened to plain pointers and
+ * sizes so that any FFI (ctypes, cgo, JNI, N-API) or the C++ adapter in
+ * INTEGRATION.md can bind it.  Each function cites the reference member it
+ * replaces.
+ *
+ * Conventions
+ *   - Every function returns an int status: BCSIM_OK (0) or a BCSIM_E_* code.
+ *     No C++ exception crosses this boundary.  The message of the last failure
+ *     on a handle (the text the reference would have put in its
+ *     std::runtime_error) is returned by bcsim_last_error().
+ *   - Inputs are copied by the callee before the call returns (the semantics of
+ *     the reference GPU algorithm, src/core/algorithm/GpuScatterers.cpp:42-46);
+ *     the caller keeps ownership of every pointer it passes.
+ *   - Vectors are float32 [n][3] row-major (x, y, z); IQ output is complex64
+ *     stored as interleaved float pairs, line-major: out[line][sample][re, im].
+ *   - One handle is not thread-safe (as the reference); distinct handles are.
+ */
+#ifndef BCSIM_GB300_H
+#define BCSIM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BCSIM_OK              0
+#define BCSIM_E_INVALID       1   /* bad argument or configuration (std::runtime_error) */
+#define BCSIM_E_NOT_CONFIGURED 2  /* simulate_lines before configuration            */
+#define BCSIM_E_CUDA          3   /* CUDA runtime failure                            */
+#define BCSIM_E_CAPACITY      4   /* caller buffer too small                         */
+#define BCSIM_E_MEMORY        5   /* device/host allocation refused                  */
+#define BCSIM_E_INTERNAL      6   /* internal invariant (std::logic_error)           */
+
+typedef struct bcsim_handle bcsim_handle;
+
+/* bcsim::Create(sim_type)  (src/core/LibBCSim.cpp:39-49).  Accepted type: "gpu".
+ * Any other string fails with "Illegal algorithm type: <type>". */
+int bcsim_create(const char* sim_type, bcsim_handle** out);
+
+/* IAlgorithm destructor. */
+int bcsim_destroy(bcsim_handle* h);
+
+/* Message of the last failed call on h ("" if none).  Valid until the next call on h.
+ * With h == NULL: the message of the calling thread's last failed bcsim_create. */
+const char* bcsim_last_error(const bcsim_handle* h);
+
+/* IAlgorithm::set_parameter (src/core/LibBCSim.hpp:51; keys of
+ * src/core/algorithm/BaseAlgorithm.cpp:48-87 and GpuAlgorithm.cpp:68-107):
+ *   verbose, sound_speed, noise_amplitude, use_arc_projection, radial_decimation,
+ *   phase_delay, gpu_device, cuda_streams, threads_per_block, store_kernel_details,
+ * plus this engine's own keys:
+ *   precision_mode ("fp64" | "reference"), fir_tail_energy, tile_lines, autotune. */
+int bcsim_set_parameter(bcsim_handle* h, const char* key, const char* value);
+
+/* IAlgorithm::get_parameter (GpuAlgorithm.cpp:761-773): num_cuda_devices,
+ * cur_device_name, and the value of any settable key.  Writes a NUL-terminated
+ * string of at most cap bytes. */
+int bcsim_get_parameter(const bcsim_handle* h, const char* key, char* buf, int cap);
+
+/* IAlgorithm::set_excitation (LibBCSim.hpp:72; ExcitationSignal BCSimConfig.hpp:79-92). */
+int bcsim_set_excitation(bcsim_handle* h, const float* samples, int num_samples, int center_index,
+                         float sampling_frequency, float demod_freq);
+
+/* IAlgorithm::set_scan_sequence (LibBCSim.hpp:69) with the Scanline checks of
+ * src/core/ScanSequence.cpp:37-70 applied to every line (elevational direction =
+ * lateral x direction, orthonormal to 1e-4).  origins/directions/lateral_dirs:
+ * float [num_lines][3]; timestamps: float [num_lines]. */
+int bcsim_set_scan_sequence(bcsim_handle* h, const float* origins, const float* directions,
+                            const float* lateral_dirs, const float* timestamps, int num_lines,
+                            float line_length);
+
+/* IAlgorithm::set_analytical_profile with a GaussianBeamProfile
+ * (LibBCSim.hpp:75; BeamProfile.hpp:52-84). */
+int bcsim_set_analytical_profile(bcsim_handle* h, float sigma_lateral, float sigma_elevational);
+
+/* IAlgorithm::set_lookup_profile with a LUTBeamProfile (LibBCSim.hpp:78;
+ * BeamProfile.hpp:88-142).  samples: float [nr][nl][ne] row-major
+ * (radial, lateral, elevational); extents are the first and last sample positions. */
+int bcsim_set_lookup_profile(bcsim_handle* h, const float* samples, int nr, int nl, int ne,
+                             float r_first, float r_last, float l_first, float l_last,
+                             float e_first, float e_last);
+
+/* IAlgorithm::clear_fixed_scatterers / add_fixed_scatterers (LibBCSim.hpp:57-60).
+ * xyza: float [n][4] = (x, y, z, amplitude), the row layout of the reference's
+ * Python binding (src/python/PythonInterface.cpp:84-101). */
+int bcsim_clear_fixed_scatterers(bcsim_handle* h);
+int bcsim_add_fixed_scatterers(bcsim_handle* h, const float* xyza, int64_t n);
+/* clear_fixed_scatterers + add_fixed_scatterers in one call. */
+int bcsim_set_fixed_scatterers(bcsim_handle* h, const float* xyza, int64_t n);
+
+/* IAlgorithm::clear_spline_scatterers / add_spline_scatterers (LibBCSim.hpp:63-66;
+ * SplineScatterers BCSimConfig.hpp:126-165).  knots: float [num_knots] with
+ * num_knots = num_cs + degree + 1; control_points: float [n][num_cs][3];
+ * amplitudes: float [n]. */
+int bcsim_clear_spline_scatterers(bcsim_handle* h);
+int bcsim_add_spline_scatterers(bcsim_handle* h, int degree, const float* knots, int num_knots,
+                                const float* control_points, const float* amplitudes, int64_t n,
+                                int num_cs);
+/* clear_spline_scatterers + add_spline_scatterers in one call. */
+int bcsim_set_spline_scatterers(bcsim_handle* h, int degree, const float* knots, int num_knots,
+                                const float* control_points, const float* amplitudes, int64_t n,
+                                int num_cs);
+
+/* IAlgorithm::get_total_num_scatterers (LibBCSim.hpp:87). */
+int bcsim_get_total_num_scatterers(const bcsim_handle* h, int64_t* out);
+
+/* Shape of the IQ output of the current configuration: num_lines lines of
+ * num_samples = ceil(ns / radial_decimation) complex samples, where
+ * ns = floor(fs * 2 * line_length / sound_speed + 0.5) (common_utils.hpp:38-41). */
+int bcsim_get_output_shape(const bcsim_handle* h, int64_t* num_lines, int64_t* num_samples);
+
+/* IAlgorithm::simulate_lines (LibBCSim.hpp:81).  out: host buffer of
+ * cap_complex complex64 values, filled as out[line][sample]; the shape is
+ * returned in num_lines / num_samples.  Blocks until the IQ is on the host. */
+int bcsim_simulate_lines(bcsim_handle* h, float* out, int64_t cap_complex,
+                         int64_t* num_lines, int64_t* num_samples);
+
+/* simulate_lines into a device buffer (complex64 [num_lines][num_samples], at
+ * least 16-byte aligned) on the handle's stream, without a host copy and
+ * without synchronising.  For callers that keep the IQ on the GPU. */
+int bcsim_simulate_lines_device(bcsim_handle* h, void* device_out, int64_t cap_complex);
+
+/* The CUDA stream (a cudaStream_t) all work of h is issued on. */
+int bcsim_get_stream(const bcsim_handle* h, void** stream);
+
+/* IAlgorithm::get_debug_data (LibBCSim.hpp:84; keys of GpuAlgorithm.cpp:196-358
+ * when store_kernel_details is on: kernel_memset_ms, fixed_projection_kernel_ms,
+ * spline_projection_kernel_ms, kernel_convolve_demodulate_ms, kernel_memcpy_ms,
+ * plus prep_sort_ms, total_ms).  Writes up to cap doubles; *n receives the count. */
+int bcsim_get_debug_data(const bcsim_handle* h, const char* key, double* out, int64_t cap, int64_t* n);
+
+/* IAlgorithm::set_logger (LibBCSim.hpp:90): fn(level, message, user) receives the
+ * messages the reference writes to its ILog (levels 0 DEBUG, 1 INFO, 2 WARNING,
+ * 3 FATAL).  fn = NULL restores the silent default (DummyLog). */
+typedef void (*bcsim_log_fn)(int level, const char* message, void* user);
+int bcsim_set_logger(bcsim_handle* h, bcsim_log_fn fn, void* user);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BCSIM_GB300_H */

@@ -1,0 +1,226 @@
+"""GB300-native COLE ultrasound line simulator.
+
+`RfSimulator` mirrors the reference's Python class `pyrfsim.RfSimulator`
+(src/python/PythonInterface.cpp:58-351): the same method names, argument
+meanings, array shapes and error messages, over the C ABI of
+include/bcsim_gb300.h.  Errors raise RuntimeError with the reference's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _capi
+
+__all__ = ["RfSimulator", "SimulatorError", "load_library"]
+
+
+class SimulatorError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+def load_library():
+    return _capi.load()
+
+
+def _f32(a, shape_msg: str, ndim: int, last: Optional[int] = None) -> np.ndarray:
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if arr.ndim != ndim:
+        raise RuntimeError(shape_msg)
+    if last is not None and arr.shape[-1] != last:
+        raise RuntimeError(shape_msg)
+    return arr
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class RfSimulator:
+    """One simulator instance (`bcsim::Create(sim_type)`, LibBCSim.cpp:39-49)."""
+
+    def __init__(self, sim_type: str = "gpu"):
+        self._lib = _capi.load()
+        h = C.c_void_p()
+        rc = self._lib.bcsim_create(sim_type.encode(), C.byref(h))
+        if rc != 0:
+            raise SimulatorError(rc, self._lib.bcsim_last_error(None).decode())
+        self._h = h
+        self._print_debug = False
+        self._log_cb = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.bcsim_destroy(h)
+            self._h = None
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise SimulatorError(rc, self._lib.bcsim_last_error(self._h).decode())
+
+    @property
+    def handle(self):
+        return self._h
+
+    # --- PythonInterface.cpp:70-78 ---
+    def set_print_debug(self, val: bool):
+        self._print_debug = bool(val)
+
+    def set_parameter(self, key: str, value: str):
+        self._check(self._lib.bcsim_set_parameter(self._h, key.encode(), str(value).encode()))
+
+    def get_parameter(self, key: str) -> str:
+        buf = C.create_string_buffer(1024)
+        self._check(self._lib.bcsim_get_parameter(self._h, key.encode(), buf, 1024))
+        return buf.value.decode()
+
+    # --- fixed scatterers, PythonInterface.cpp:80-101: data [N, 4] ---
+    def clear_fixed_scatterers(self):
+        self._check(self._lib.bcsim_clear_fixed_scatterers(self._h))
+
+    def add_fixed_scatterers(self, data):
+        arr = np.asarray(data)
+        if arr.ndim != 2 or arr.shape[1] != 4:
+            raise RuntimeError("add_fixed_scatterers : Number of columns must be four")
+        arr = np.ascontiguousarray(arr, dtype=np.float32)
+        self._check(self._lib.bcsim_add_fixed_scatterers(self._h, _ptr(arr), arr.shape[0]))
+
+    # --- spline scatterers, PythonInterface.cpp:103-177 ---
+    def clear_spline_scatterers(self):
+        self._check(self._lib.bcsim_clear_spline_scatterers(self._h))
+
+    def add_spline_scatterers(self, spline_degree: int, knot_vector, control_points, amplitudes):
+        knots = np.asarray(knot_vector)
+        if knots.ndim != 1:
+            raise RuntimeError("add_spline_scatterers : invalid knot vector rank")
+        cps = np.asarray(control_points)
+        if cps.ndim != 3:
+            raise RuntimeError("add_spline_scatterers : invalid control_points rank")
+        n, k = cps.shape[0], cps.shape[1]
+        if len(knots) != k + int(spline_degree) + 1:
+            raise RuntimeError("add_spline_scatterers : mismatch in number of nodes, degree and control points")
+        if cps.shape[2] != 3:
+            raise RuntimeError("add_spline_scatterers : size of dimension 3 must be three (x,y,z)")
+        amps = np.asarray(amplitudes)
+        if amps.shape[0] != n:
+            raise RuntimeError("Mismatch between control_points and amplitudes")
+        knots = np.ascontiguousarray(knots, np.float32)
+        cps = np.ascontiguousarray(cps, np.float32)
+        amps = np.ascontiguousarray(amps, np.float32)
+        self._check(self._lib.bcsim_add_spline_scatterers(self._h, int(spline_degree), _ptr(knots), len(knots),
+                                                          _ptr(cps), _ptr(amps), n, k))
+
+    # --- scan sequence, PythonInterface.cpp:179-220 ---
+    def set_scan_sequence(self, origins, directions, line_length, lateral_dirs, timestamps):
+        o = np.asarray(origins)
+        d = np.asarray(directions)
+        l = np.asarray(lateral_dirs)
+        t = np.asarray(timestamps)
+        if o.ndim != 2 or d.ndim != 2 or l.ndim != 2 or t.ndim != 1:
+            raise RuntimeError("set_scan_sequence(): Invalid rank.")
+        n = o.shape[0]
+        if n != d.shape[0] or n != l.shape[0]:
+            raise RuntimeError("set_scan_sequence(): Mismatch in number of rows.")
+        o, d, l, t = (np.ascontiguousarray(x, np.float32) for x in (o, d, l, t))
+        self._check(self._lib.bcsim_set_scan_sequence(self._h, _ptr(o), _ptr(d), _ptr(l), _ptr(t), n,
+                                                      float(line_length)))
+
+    # --- excitation, PythonInterface.cpp:222-241 ---
+    def set_excitation(self, samples, center_index: int, fs: float, demod_freq: float):
+        s = np.asarray(samples)
+        if s.ndim != 1:
+            raise RuntimeError("set_excitation: samples should be one-dimensional")
+        s = np.ascontiguousarray(s, np.float32)
+        self._check(self._lib.bcsim_set_excitation(self._h, _ptr(s), len(s), int(center_index), float(fs),
+                                                   float(demod_freq)))
+
+    # --- beam profiles, PythonInterface.cpp:243-297 ---
+    def set_analytical_beam_profile(self, sigma_lateral: float, sigma_elevational: float):
+        self._check(self._lib.bcsim_set_analytical_profile(self._h, float(sigma_lateral), float(sigma_elevational)))
+
+    def set_lut_beam_profile(self, r_min, r_max, l_min, l_max, e_min, e_max, samples):
+        s = np.asarray(samples)
+        if s.ndim != 3:
+            raise RuntimeError("Number of sample dimensions must be three.")
+        s = np.ascontiguousarray(s, np.float32)
+        self._check(self._lib.bcsim_set_lookup_profile(self._h, _ptr(s), s.shape[0], s.shape[1], s.shape[2],
+                                                       r_min, r_max, l_min, l_max, e_min, e_max))
+
+    # --- simulate, PythonInterface.cpp:299-318: returns [num_samples, num_lines] complex64 ---
+    def simulate_lines(self) -> np.ndarray:
+        return self.simulate_lines_line_major().T
+
+    def simulate_lines_line_major(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """IQ as [num_lines, num_samples] complex64 (the C ABI's layout)."""
+        L, nd = C.c_int64(), C.c_int64()
+        self._check(self._lib.bcsim_get_output_shape(self._h, C.byref(L), C.byref(nd)))
+        if out is None or out.shape != (L.value, nd.value) or out.dtype != np.complex64:
+            out = np.empty((L.value, nd.value), np.complex64)
+        self._check(self._lib.bcsim_simulate_lines(self._h, out.ctypes.data_as(C.POINTER(C.c_float)), out.size,
+                                                   C.byref(L), C.byref(nd)))
+        return out
+
+    def simulate_lines_device(self, device_ptr: int, capacity: int):
+        """IQ into a device buffer of `capacity` complex64 values (no host copy)."""
+        self._check(self._lib.bcsim_simulate_lines_device(self._h, C.c_void_p(device_ptr), int(capacity)))
+
+    def output_shape(self):
+        L, nd = C.c_int64(), C.c_int64()
+        self._check(self._lib.bcsim_get_output_shape(self._h, C.byref(L), C.byref(nd)))
+        return L.value, nd.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self._lib.bcsim_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    # --- PythonInterface.cpp:320-337 ---
+    def get_debug_data(self, identifier: str):
+        n = C.c_int64()
+        buf = (C.c_double * 65536)()
+        self._check(self._lib.bcsim_get_debug_data(self._h, identifier.encode(), buf, 65536, C.byref(n)))
+        return [buf[i] for i in range(n.value)]
+
+    def get_total_num_scatterers(self) -> int:
+        n = C.c_int64()
+        self._check(self._lib.bcsim_get_total_num_scatterers(self._h, C.byref(n)))
+        return n.value
+
+    def set_logger(self, fn):
+        """fn(level: int, message: str) receives the engine's log messages; None silences."""
+        if fn is None:
+            self._log_cb = None
+            self._check(self._lib.bcsim_set_logger(self._h, _capi.LOG_FN(), None))
+            return
+        self._log_cb = _capi.LOG_FN(lambda lvl, msg, user: fn(int(lvl), msg.decode()))
+        self._check(self._lib.bcsim_set_logger(self._h, self._log_cb, None))
+
+
+def configure_job(sim: RfSimulator, job, precision_mode: str = "fp64"):
+    """Configure a simulator from a workloads.Job (synthetic seeded inputs)."""
+    sim.set_parameter("sound_speed", repr(float(np.float32(job.sound_speed))))
+    sim.set_parameter("use_arc_projection", "on" if job.arc else "off")
+    sim.set_parameter("phase_delay", "on" if job.phase_delay else "off")
+    sim.set_parameter("radial_decimation", str(job.decimation))
+    sim.set_parameter("precision_mode", precision_mode)
+    sim.set_excitation(job.taps, job.center_index, job.fs, job.demod_freq)
+    s = job.scan
+    sim.set_scan_sequence(s.origins, s.directions, s.line_length, s.lateral_dirs, s.timestamps)
+    b = job.beam
+    if hasattr(b, "sigma_lateral"):
+        sim.set_analytical_beam_profile(b.sigma_lateral, b.sigma_elevational)
+    else:
+        sim.set_lut_beam_profile(b.r_range[0], b.r_range[1], b.l_range[0], b.l_range[1], b.e_range[0], b.e_range[1],
+                                 b.samples)
+    sim.clear_fixed_scatterers()
+    for f in job.fixed:
+        sim.add_fixed_scatterers(f.xyza)
+    sim.clear_spline_scatterers()
+    for sp in job.splines:
+        sim.add_spline_scatterers(sp.degree, sp.knots, sp.control_points, sp.amplitudes)
+    return sim

@@ -1,0 +1,826 @@
+// engine.cpp -- host side of the GB300 COLE simulator (see engine.hpp).
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <sstream>
+
+#include "../../include/bcsim_gb300.h"
+#include "host_dsp.hpp"
+
+namespace bcsim_gb300 {
+
+#define BCSIM_CUDA(call)                                                                                    \
+    do {                                                                                                    \
+        cudaError_t e_ = (call);                                                                            \
+        if (e_ != cudaSuccess) {                                                                            \
+            throw SimError(BCSIM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" __FILE__ \
+                                             ":" + std::to_string(__LINE__) + ")");                          \
+        }                                                                                                   \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// DeviceBuffer
+// ---------------------------------------------------------------------------
+DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) {
+        release();
+        ptr_ = o.ptr_;
+        bytes_ = o.bytes_;
+        o.ptr_ = nullptr;
+        o.bytes_ = 0;
+    }
+    return *this;
+}
+
+DeviceBuffer::~DeviceBuffer() { release(); }
+
+void DeviceBuffer::release() {
+    if (ptr_) cudaFree(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+}
+
+void DeviceBuffer::reserve(size_t bytes) {
+    if (bytes <= bytes_ && ptr_) return;
+    release();
+    if (bytes == 0) bytes = 16;
+    const cudaError_t e = cudaMalloc(&ptr_, bytes);
+    if (e != cudaSuccess) {
+        ptr_ = nullptr;
+        cudaGetLastError();
+        throw SimError(BCSIM_E_MEMORY, std::string("device allocation of ") + std::to_string(bytes) +
+                                           " bytes failed: " + cudaGetErrorString(e));
+    }
+    bytes_ = bytes;
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static bool parse_bool(const std::string& v, bool* out) {
+    if (v == "on" || v == "true") { *out = true; return true; }
+    if (v == "off" || v == "false") { *out = false; return true; }
+    return false;
+}
+
+static float fdot(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+static std::string fmt_double(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%.17g", v);
+    return buf;
+}
+
+Simulator::Simulator() = default;
+
+Simulator::~Simulator() {
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Simulator::log(int level, const std::string& msg) const {
+    if (log_fn_) log_fn_(level, msg.c_str(), log_user_);
+}
+
+void Simulator::ensure_device() {
+    if (device_ready_) return;
+    int count = 0;
+    BCSIM_CUDA(cudaGetDeviceCount(&count));
+    if (device_ < 0 || device_ >= count) throw SimError(BCSIM_E_INVALID, "illegal CUDA device number");
+    BCSIM_CUDA(cudaSetDevice(device_));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    device_ready_ = true;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device_) == cudaSuccess) {
+        std::ostringstream ss;
+        ss << "=== CUDA Device " << device_ << ": " << prop.name << " (compute capability " << prop.major << "."
+           << prop.minor << ", " << prop.multiProcessorCount << " SMs)";
+        log(1, ss.str());
+    }
+}
+
+cudaStream_t Simulator::stream() {
+    ensure_device();
+    return stream_;
+}
+
+// ---------------------------------------------------------------------------
+// parameters (BaseAlgorithm.cpp:48-87, GpuAlgorithm.cpp:68-107)
+// ---------------------------------------------------------------------------
+void Simulator::set_parameter(const std::string& key, const std::string& value) {
+    bool b = false;
+    if (key == "verbose") {
+        verbose_ = std::stoi(value);
+    } else if (key == "sound_speed") {
+        const float v = std::stof(value);
+        if (v <= 0) throw SimError(BCSIM_E_INVALID, "illegal sound speed");
+        sound_speed_ = v;
+    } else if (key == "noise_amplitude") {
+        const float v = std::stof(value);
+        if (v != 0.0f) throw SimError(BCSIM_E_INVALID, "noise_amplitude: only 0 is supported by this engine");
+        noise_amplitude_ = v;
+    } else if (key == "use_arc_projection") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        arc_ = b;
+    } else if (key == "radial_decimation") {
+        const int v = std::stoi(value);
+        if (v <= 0) throw SimError(BCSIM_E_INVALID, "illegal radial decimation value");
+        if (v != decimation_) tables_valid_ = false;
+        decimation_ = v;
+    } else if (key == "phase_delay") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        phase_delay_ = b;
+    } else if (key == "gpu_device") {
+        if (device_ready_) throw SimError(BCSIM_E_INVALID, "cannot change CUDA device now");
+        int count = 0;
+        BCSIM_CUDA(cudaGetDeviceCount(&count));
+        const int v = std::stoi(value);
+        if (v < 0 || v >= count) throw SimError(BCSIM_E_INVALID, "illegal device number");
+        device_ = v;
+    } else if (key == "cuda_streams") {
+        const int v = std::stoi(value);
+        if (v > 2) throw SimError(BCSIM_E_INVALID, "number of CUDA streams exceeds MAX_NUM_CUDA_STREAMS");
+        if (v <= 0) throw SimError(BCSIM_E_INVALID, "number of CUDA streams must be more than zero");
+        cuda_streams_ = v;
+    } else if (key == "threads_per_block") {
+        const int v = std::stoi(value);
+        if (v <= 0) throw SimError(BCSIM_E_INVALID, "invalid number of threads per block");
+        threads_per_block_ = v;
+    } else if (key == "store_kernel_details") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid value");
+        store_details_ = b;
+    } else if (key == "precision_mode") {
+        int m;
+        if (value == "fp64") m = MODE_FP64;
+        else if (value == "reference") m = MODE_REFERENCE;
+        else throw SimError(BCSIM_E_INVALID, "invalid value for precision_mode (fp64 | reference)");
+        if (m != mode_) tables_valid_ = false;
+        mode_ = m;
+    } else if (key == "fir_tail_energy") {
+        const double v = std::stod(value);
+        if (!(v >= 0.0 && v < 1.0)) throw SimError(BCSIM_E_INVALID, "fir_tail_energy must be in [0, 1)");
+        if (v != fir_tail_) tables_valid_ = false;
+        fir_tail_ = v;
+    } else if (key == "tile_lines") {
+        const int v = std::stoi(value);
+        if (v < 0) throw SimError(BCSIM_E_INVALID, "tile_lines must be >= 0");
+        tile_lines_ = v;
+    } else {
+        throw SimError(BCSIM_E_INVALID, std::string("illegal parameter name: '") + key + "'");
+    }
+}
+
+std::string Simulator::get_parameter(const std::string& key) const {
+    if (key == "num_cuda_devices") {
+        int count = 0;
+        BCSIM_CUDA(cudaGetDeviceCount(&count));
+        return std::to_string(count);
+    }
+    if (key == "cur_device_name") {
+        cudaDeviceProp prop;
+        BCSIM_CUDA(cudaGetDeviceProperties(&prop, device_));
+        return prop.name;
+    }
+    if (key == "verbose") return std::to_string(verbose_);
+    if (key == "sound_speed") return fmt_double(sound_speed_);
+    if (key == "noise_amplitude") return fmt_double(noise_amplitude_);
+    if (key == "use_arc_projection") return arc_ ? "on" : "off";
+    if (key == "radial_decimation") return std::to_string(decimation_);
+    if (key == "phase_delay") return phase_delay_ ? "on" : "off";
+    if (key == "gpu_device") return std::to_string(device_);
+    if (key == "cuda_streams") return std::to_string(cuda_streams_);
+    if (key == "threads_per_block") return std::to_string(threads_per_block_);
+    if (key == "store_kernel_details") return store_details_ ? "on" : "off";
+    if (key == "precision_mode") return mode_ == MODE_FP64 ? "fp64" : "reference";
+    if (key == "fir_tail_energy") return fmt_double(fir_tail_);
+    if (key == "tile_lines") return std::to_string(tile_lines_);
+    if (key == "fir_taps") return std::to_string(tap_count_);
+    throw SimError(BCSIM_E_INVALID, "Illegal key: " + key);
+}
+
+// ---------------------------------------------------------------------------
+// configuration
+// ---------------------------------------------------------------------------
+void Simulator::set_excitation(const float* samples, int n, int center_index, float fs, float demod_freq) {
+    if (n < 0 || (n > 0 && !samples)) throw SimError(BCSIM_E_INVALID, "set_excitation: invalid samples");
+    taps_.assign(samples, samples + n);
+    center_ = center_index;
+    fs_ = fs;
+    fd_ = demod_freq;
+    excitation_set_ = true;
+    tables_valid_ = false;
+    log(1, "Number of excitation samples: " + std::to_string(n));
+}
+
+void Simulator::set_scan_sequence(const float* origins, const float* dirs, const float* lats, const float* timestamps,
+                                  int num_lines, float line_length) {
+    if (num_lines < 0 || (num_lines > 0 && (!origins || !dirs || !lats || !timestamps)))
+        throw SimError(BCSIM_E_INVALID, "set_scan_sequence(): Invalid rank.");
+    // Scanline construction and validation (ScanSequence.cpp:37-70)
+    std::vector<LineGeom> lines(static_cast<size_t>(num_lines));
+    for (int i = 0; i < num_lines; i++) {
+        LineGeom& g = lines[i];
+        for (int k = 0; k < 3; k++) {
+            g.o[k] = origins[3 * i + k];
+            g.d[k] = dirs[3 * i + k];
+            g.l[k] = lats[3 * i + k];
+        }
+        // elevational = lateral x direction (vector3.hpp:97-103)
+        g.e[0] = g.l[1] * g.d[2] - g.d[1] * g.l[2];
+        g.e[1] = g.d[0] * g.l[2] - g.l[0] * g.d[2];
+        g.e[2] = g.l[0] * g.d[1] - g.d[0] * g.l[1];
+        const float thr = 1e-4f;
+        if (std::abs(fdot(g.d, g.l)) >= thr || std::abs(fdot(g.l, g.e)) >= thr || std::abs(fdot(g.e, g.d)) >= thr)
+            throw SimError(BCSIM_E_INVALID, "Invalid Scanline: Not orthogonal unit vectors");
+        const float nd = std::sqrt(fdot(g.d, g.d)), nl = std::sqrt(fdot(g.l, g.l)), ne = std::sqrt(fdot(g.e, g.e));
+        if (std::abs(nd - 1.0) >= thr || std::abs(nl - 1.0) >= thr || std::abs(ne - 1.0) >= thr)
+            throw SimError(BCSIM_E_INVALID, "Invalid Scanline: Not unit length vectors");
+    }
+    // CpuAlgorithm.cpp:258-260
+    if (!excitation_set_) throw SimError(BCSIM_E_INVALID, "Excitation must be configured before scan sequence");
+    lines_ = std::move(lines);
+    timestamps_.assign(timestamps, timestamps + num_lines);
+    num_lines_ = num_lines;
+    line_length_ = line_length;
+    ns_ = num_rf_samples(sound_speed_, line_length, fs_);
+    shared_origin_ = true;
+    timestamps_equal_ = true;
+    for (int i = 1; i < num_lines; i++) {
+        if (std::memcmp(lines_[i].o, lines_[0].o, sizeof(lines_[0].o)) != 0) shared_origin_ = false;
+        if (std::memcmp(&timestamps_[i], &timestamps_[0], sizeof(float)) != 0) timestamps_equal_ = false;
+    }
+    scan_set_ = true;
+    lines_valid_ = false;
+    tables_valid_ = false;
+}
+
+void Simulator::set_analytical_profile(float sigma_lateral, float sigma_elevational) {
+    log(1, "Setting analytical beam profile for GPU algorithm");
+    beam_type_ = BEAM_GAUSSIAN;
+    sigma_l_ = sigma_lateral;
+    sigma_e_ = sigma_elevational;
+}
+
+void Simulator::set_lookup_profile(const float* samples, int nr, int nl, int ne, float r0, float r1, float l0,
+                                   float l1, float e0, float e1) {
+    log(1, "Setting LUT profile for GPU algorithm");
+    // LUTBeamProfile constructor checks (BeamProfile.cpp:64-66)
+    if (nr <= 1) throw SimError(BCSIM_E_INVALID, "Too few radial samples");
+    if (nl <= 1) throw SimError(BCSIM_E_INVALID, "Too few lateral samples");
+    if (ne <= 1) throw SimError(BCSIM_E_INVALID, "Too few elevational samples");
+    if (!samples) throw SimError(BCSIM_E_INVALID, "set_lookup_profile: samples is null");
+    const size_t total = (size_t)nr * nl * ne;
+    lut_.assign(samples, samples + total);
+    lut_nr_ = nr; lut_nl_ = nl; lut_ne_ = ne;
+    lut_ext_[0] = r0; lut_ext_[1] = r1; lut_ext_[2] = l0; lut_ext_[3] = l1; lut_ext_[4] = e0; lut_ext_[5] = e1;
+    lut_absmax_ = 0.0;
+    for (float v : lut_) lut_absmax_ = std::max(lut_absmax_, (double)std::fabs(v));
+    beam_type_ = BEAM_LUT;
+    lut_uploaded_ = false;
+}
+
+void Simulator::clear_fixed_scatterers() {
+    fixed_n_ = 0;
+    num_fixed_sets_ = 0;
+    fixed_sum_abs_ = 0.0;
+    amplitude_nonfinite_ = false;
+    for (const auto& s : splines_) (void)s;
+}
+
+void Simulator::add_fixed_scatterers(const float* xyza, int64_t n) {
+    if (n < 0 || (n > 0 && !xyza)) throw SimError(BCSIM_E_INVALID, "add_fixed_scatterers: invalid data");
+    ensure_device();
+    if (n > 0) {
+        const size_t need = (size_t)(fixed_n_ + n) * sizeof(float4);
+        if (need > fixed_xyza_.bytes()) {
+            DeviceBuffer grown;
+            grown.reserve(std::max(need, fixed_xyza_.bytes() * 3 / 2));
+            if (fixed_n_ > 0)
+                BCSIM_CUDA(cudaMemcpyAsync(grown.get(), fixed_xyza_.get(), (size_t)fixed_n_ * sizeof(float4),
+                                           cudaMemcpyDeviceToDevice, stream_));
+            BCSIM_CUDA(cudaStreamSynchronize(stream_));
+            fixed_xyza_ = std::move(grown);
+        }
+        BCSIM_CUDA(cudaMemcpyAsync(fixed_xyza_.as<float4>() + fixed_n_, xyza, (size_t)n * sizeof(float4),
+                                   cudaMemcpyHostToDevice, stream_));
+        double s = 0.0;
+        for (int64_t i = 0; i < n; i++) {
+            const float a = xyza[4 * i + 3];
+            if (!std::isfinite(a)) amplitude_nonfinite_ = true;
+            else s += std::fabs((double)a);
+        }
+        fixed_sum_abs_ += s;
+        BCSIM_CUDA(cudaStreamSynchronize(stream_));
+    }
+    fixed_n_ += n;
+    num_fixed_sets_ += 1;
+    if (verbose_) log(1, "Number of fixed scatterers: " + std::to_string(fixed_n_));
+}
+
+void Simulator::clear_spline_scatterers() { splines_.clear(); }
+
+void Simulator::add_spline_scatterers(int degree, const float* knots, int num_knots, const float* cps,
+                                      const float* amps, int64_t n, int num_cs) {
+    if (n < 0 || num_cs < 0 || num_knots < 0 || (n > 0 && (!cps || !amps)) || (num_knots > 0 && !knots))
+        throw SimError(BCSIM_E_INVALID, "add_spline_scatterers: invalid data");
+    // src/python/PythonInterface.cpp:150-153
+    if (num_knots != num_cs + degree + 1)
+        throw SimError(BCSIM_E_INVALID, "add_spline_scatterers : mismatch in number of nodes, degree and control points");
+    if (degree < 0 || degree > MAX_SPLINE_DEGREE)
+        throw SimError(BCSIM_E_INVALID, "add_spline_scatterers : spline degree must be in [0, " +
+                                            std::to_string(MAX_SPLINE_DEGREE) + "]");
+    ensure_device();
+    SplineDataset ds;
+    ds.degree = degree;
+    ds.num_cs = num_cs;
+    ds.knots.assign(knots, knots + num_knots);
+    ds.n = n;
+    if (n > 0 && num_cs > 0) {
+        // [n][K][3] -> [K][n] float4
+        std::vector<float4> t((size_t)num_cs * n);
+        for (int64_t i = 0; i < n; i++)
+            for (int k = 0; k < num_cs; k++) {
+                const float* q = cps + (i * num_cs + k) * 3;
+                t[(size_t)k * n + i] = make_float4(q[0], q[1], q[2], 0.0f);
+            }
+        ds.cps.reserve(t.size() * sizeof(float4));
+        BCSIM_CUDA(cudaMemcpy(ds.cps.get(), t.data(), t.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    }
+    if (n > 0) {
+        ds.amps.reserve((size_t)n * sizeof(float));
+        BCSIM_CUDA(cudaMemcpy(ds.amps.get(), amps, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+        for (int64_t i = 0; i < n; i++) {
+            if (!std::isfinite(amps[i])) amplitude_nonfinite_ = true;
+            else ds.sum_abs_amp += std::fabs((double)amps[i]);
+        }
+    }
+    splines_.push_back(std::move(ds));
+    if (verbose_) log(1, "Number of spline datasets: " + std::to_string(splines_.size()));
+}
+
+int64_t Simulator::total_num_scatterers() const {
+    int64_t t = fixed_n_;
+    for (const auto& s : splines_) t += s.n;
+    return t;
+}
+
+void Simulator::output_shape(int64_t* lines, int64_t* samples) const {
+    if (!scan_set_) throw SimError(BCSIM_E_NOT_CONFIGURED, "Scan sequence not configured.");
+    if (lines) *lines = num_lines_;
+    if (samples) *samples = (ns_ + decimation_ - 1) / decimation_;
+}
+
+// CpuAlgorithm.cpp:385-398 and GpuAlgorithm.cpp:157-163
+void Simulator::throw_if_not_configured() const {
+    if (!scan_set_) throw SimError(BCSIM_E_NOT_CONFIGURED, "Scan sequence not configured.");
+    if (!excitation_set_) throw SimError(BCSIM_E_NOT_CONFIGURED, "Excitation not configured.");
+    if (beam_type_ == 0) throw SimError(BCSIM_E_NOT_CONFIGURED, "Beam profile not configured.");
+    if (total_num_scatterers() == 0) throw SimError(BCSIM_E_NOT_CONFIGURED, "no scatterers are configured");
+    if (num_lines_ < 1) throw SimError(BCSIM_E_NOT_CONFIGURED, "No scanlines in scansequence");
+}
+
+std::vector<double> Simulator::get_debug_data(const std::string& key) const {
+    auto it = debug_.find(key);
+    if (it == debug_.end()) throw SimError(BCSIM_E_INVALID, "invalid debug data key: " + key);
+    return it->second;
+}
+
+// ---------------------------------------------------------------------------
+// derived tables
+// ---------------------------------------------------------------------------
+void Simulator::prepare_excitation_tables() {
+    if (tables_valid_) return;
+    const int64_t ntaps = (int64_t)taps_.size();
+    M_ = next_power_of_two(ns_ + ntaps - 1);
+    nd_ = (ns_ + decimation_ - 1) / decimation_;
+    if (center_ < 0 || (int64_t)center_ + (nd_ - 1) * decimation_ >= M_)
+        throw SimError(BCSIM_E_INVALID, "excitation center index outside the convolution buffer");
+    const auto ha = analytic_pulse(taps_, M_);
+    choose_tap_window(ha, (int)ntaps, fir_tail_, &tap_start_, &tap_count_);
+    std::vector<float2> taps((size_t)tap_count_);
+    for (int64_t w = 0; w < tap_count_; w++) {
+        const int64_t n = ((tap_start_ + w) % M_ + M_) % M_;
+        taps[w] = make_float2((float)ha[n].real(), (float)ha[n].imag());
+    }
+    taps_dev_.reserve(taps.size() * sizeof(float2));
+    BCSIM_CUDA(cudaMemcpyAsync(taps_dev_.get(), taps.data(), taps.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
+    const auto dm = demod_factors(fd_, fs_, decimation_, nd_, mode_ == MODE_REFERENCE);
+    demod_dev_.reserve(dm.size() * sizeof(float2));
+    BCSIM_CUDA(cudaMemcpyAsync(demod_dev_.get(), dm.data(), dm.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));
+    tables_valid_ = true;
+    log(0, "FIR window: start " + std::to_string(tap_start_) + ", taps " + std::to_string(tap_count_) + ", M " +
+               std::to_string(M_));
+}
+
+void Simulator::prepare_lines() {
+    if (lines_valid_) return;
+    lines_dev_.reserve(std::max<size_t>(1, lines_.size()) * sizeof(LineGeom));
+    if (!lines_.empty())
+        BCSIM_CUDA(cudaMemcpyAsync(lines_dev_.get(), lines_.data(), lines_.size() * sizeof(LineGeom),
+                                   cudaMemcpyHostToDevice, stream_));
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));
+    lines_valid_ = true;
+}
+
+double Simulator::fixed_point_bound() const {
+    double s = fixed_sum_abs_;
+    for (const auto& d : splines_) s += d.sum_abs_amp;
+    const double wmax = beam_type_ == BEAM_LUT ? lut_absmax_ : 1.0;
+    return s * wmax;
+}
+
+// Packed LUT: at (r, l, e) the corners (c[r][l][e], c[r][l][e+1], c[r+1][l][e],
+// c[r+1][l][e+1]), zero past the last sample.
+static std::vector<float4> pack_lut(const std::vector<float>& c, int nr, int nl, int ne) {
+    std::vector<float4> p((size_t)nr * nl * ne);
+    auto at = [&](int r, int l, int e) -> float {
+        if (r >= nr || l >= nl || e >= ne) return 0.0f;
+        return c[((size_t)r * nl + l) * ne + e];
+    };
+    for (int r = 0; r < nr; r++)
+        for (int l = 0; l < nl; l++)
+            for (int e = 0; e < ne; e++)
+                p[((size_t)r * nl + l) * ne + e] = make_float4(at(r, l, e), at(r, l, e + 1), at(r + 1, l, e), at(r + 1, l, e + 1));
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// simulate
+// ---------------------------------------------------------------------------
+namespace {
+struct EventTimer {
+    bool on;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer(bool enabled, cudaStream_t st) : on(enabled), s(st) {
+        if (on) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, s);
+        }
+    }
+    ~EventTimer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    void restart() { if (on) cudaEventRecord(a, s); }
+    double stop() {
+        if (!on) return 0.0;
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    }
+};
+}  // namespace
+
+void Simulator::simulate(float2* dev_out, float* host_out) {
+    throw_if_not_configured();
+    if (amplitude_nonfinite_) throw SimError(BCSIM_E_INVALID, "Nan in scatterer projection.");
+    ensure_device();
+    const cudaStream_t st = stream_;
+    const int L = num_lines_;
+    const int ns = (int)ns_;
+    if (ns_ <= 0) throw SimError(BCSIM_E_INVALID, "line length gives no RF samples");
+    if (ns_ >= (int64_t)1 << 30) throw SimError(BCSIM_E_INVALID, "too many RF samples per line");
+    prepare_excitation_tables();
+    prepare_lines();
+    if (store_details_) debug_.clear();
+    EventTimer total(store_details_, st);
+    EventTimer timer(store_details_, st);
+
+    // beam
+    BeamDev b;
+    std::memset(&b, 0, sizeof(b));
+    b.type = beam_type_;
+    if (beam_type_ == BEAM_GAUSSIAN) {
+        const double log2e = 1.4426950408889634;
+        b.gl = (float)(log2e / (2.0 * (double)sigma_l_ * (double)sigma_l_));
+        b.ge = (float)(log2e / (2.0 * (double)sigma_e_ * (double)sigma_e_));
+        b.two_sl2 = 2 * sigma_l_ * sigma_l_;
+        b.two_se2 = 2 * sigma_e_ * sigma_e_;
+    } else {
+        if (!lut_uploaded_) {
+            const auto packed = pack_lut(lut_, lut_nr_, lut_nl_, lut_ne_);
+            lut4_.reserve(packed.size() * sizeof(float4));
+            BCSIM_CUDA(cudaMemcpyAsync(lut4_.get(), packed.data(), packed.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+            BCSIM_CUDA(cudaStreamSynchronize(st));
+            lut_uploaded_ = true;
+        }
+        b.lut4 = lut4_.as<float4>();
+        b.nr = lut_nr_; b.nl = lut_nl_; b.ne = lut_ne_;
+        b.rf = lut_ext_[0]; b.lf = lut_ext_[2]; b.ef = lut_ext_[4];
+        if (mode_ == MODE_FP64) {
+            b.dr = ((double)lut_ext_[1] - (double)lut_ext_[0]) / (lut_nr_ - 1);
+            b.dl = ((double)lut_ext_[3] - (double)lut_ext_[2]) / (lut_nl_ - 1);
+            b.de = ((double)lut_ext_[5] - (double)lut_ext_[4]) / (lut_ne_ - 1);
+        } else {
+            // BeamProfile.cpp:72-74: float difference divided by an int
+            b.dr = (double)((lut_ext_[1] - lut_ext_[0]) / (lut_nr_ - 1));
+            b.dl = (double)((lut_ext_[3] - lut_ext_[2]) / (lut_nl_ - 1));
+            b.de = (double)((lut_ext_[5] - lut_ext_[4]) / (lut_ne_ - 1));
+        }
+        b.inv_dr = (float)(1.0 / b.dr);
+        b.inv_dl = (float)(1.0 / b.dl);
+        b.inv_de = (float)(1.0 / b.de);
+    }
+
+    // simulation constants
+    SimParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.ns = ns;
+    p.num_lines = L;
+    p.phase_delay = phase_delay_ ? 1 : 0;
+    p.arc = arc_ ? 1 : 0;
+    p.mode = mode_;
+    p.fs = fs_; p.c = sound_speed_; p.fd = fd_;
+    p.fs_d = fs_; p.c_d = sound_speed_; p.fd_d = fd_;
+    const double k = 2.0 * (double)fs_ / (double)sound_speed_;
+    p.k_hi = (float)k;
+    p.k_lo = (float)(k - (double)p.k_hi);
+    p.two_pi_fd_over_fs = (float)(6.283185307179586 * (double)fd_ / (double)fs_);
+    const double bound = fixed_point_bound();
+    int S = 0;
+    if (bound > 0.0 && std::isfinite(bound)) S = (int)std::floor(61.0 - std::log2(bound * 1.001));
+    S = std::max(-100, std::min(100, S));
+    p.log2scale = S;
+    p.scale = std::ldexp(1.0f, S);
+
+    const int stride = phase_delay_ ? 2 : 1;
+    const size_t bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
+    bins_.reserve(bins_bytes);
+    timer.restart();
+    BCSIM_CUDA(cudaMemsetAsync(bins_.get(), 0, bins_bytes, st));
+    if (store_details_) debug_["kernel_memset_ms"].push_back(timer.stop());
+    unsigned long long* bins = bins_.as<unsigned long long>();
+    const LineGeom* lines_d = lines_dev_.as<LineGeom>();
+
+    // per-line spline knot intervals and basis (CpuAlgorithm.cpp:101-133)
+    struct SplineLines {
+        std::vector<int> mu;
+        std::vector<LineBasis> basis;
+    };
+    std::vector<SplineLines> spl(splines_.size());
+    for (size_t d = 0; d < splines_.size(); d++) {
+        const SplineDataset& ds = splines_[d];
+        if (ds.n == 0) continue;
+        if (ds.num_cs <= ds.degree) throw SimError(BCSIM_E_INVALID, "too few spline control points for given degree");
+        spl[d].mu.resize(L);
+        spl[d].basis.resize(L);
+        for (int i = 0; i < L; i++) {
+            const float t = timestamps_[i];
+            const int mu = knot_interval(ds.knots, t);
+            if (mu < 0) throw SimError(BCSIM_E_INVALID, "compute_knot_interval : could not determine knot interval");
+            const int lo = mu - ds.degree;
+            if (lo < 0 || mu >= ds.num_cs) throw SimError(BCSIM_E_INVALID, "spline evaluation index out of range");
+            LineBasis lb;
+            std::memset(&lb, 0, sizeof(lb));
+            for (int j = 0; j < ds.num_cs; j++) {
+                double v;
+                if (mode_ == MODE_FP64) v = bspline_basis_d(j, ds.degree, (double)t, ds.knots);
+                else v = bspline_basis_f(j, ds.degree, t, ds.knots);
+                if (j < lo || j > mu) {
+                    // sanity_check_spline_lower_upper_bound (common_utils.hpp:51-60)
+                    if (std::fabs(v) > 1e-6) throw SimError(BCSIM_E_INVALID, "b-spline basis bounds failed sanity check");
+                } else {
+                    const float hi = (float)v;
+                    lb.hi[j - lo] = hi;
+                    lb.lo[j - lo] = mode_ == MODE_FP64 ? (float)(v - (double)hi) : 0.0f;
+                }
+            }
+            spl[d].mu[i] = mu;
+            spl[d].basis[i] = lb;
+        }
+    }
+
+    const bool shared = shared_origin_ && arc_;
+    // splines go through the shared path when every line sees them at one time
+    std::vector<char> spline_shared(splines_.size(), 0);
+    int64_t n_shared = shared ? fixed_n_ : 0;
+    if (shared && timestamps_equal_) {
+        for (size_t d = 0; d < splines_.size(); d++) {
+            if (splines_[d].n > 0) {
+                spline_shared[d] = 1;
+                n_shared += splines_[d].n;
+            }
+        }
+    }
+
+    // line tiles for the per-pair kernel
+    auto make_tiles = [&](const std::vector<int>* mu, std::vector<int>& ids, std::vector<LineTile>& tiles) {
+        ids.resize(L);
+        std::iota(ids.begin(), ids.end(), 0);
+        if (mu) std::stable_sort(ids.begin(), ids.end(), [&](int a, int c) { return (*mu)[a] < (*mu)[c]; });
+        const int per = tile_lines_ > 0 ? tile_lines_ : 8;
+        tiles.clear();
+        int i = 0;
+        while (i < L) {
+            LineTile t;
+            t.first = i;
+            t.mu = mu ? (*mu)[ids[i]] : 0;
+            t.pad = 0;
+            int j = i;
+            while (j < L && j - i < per && (!mu || (*mu)[ids[j]] == t.mu)) j++;
+            t.count = j - i;
+            tiles.push_back(t);
+            i = j;
+        }
+    };
+    // upload tiles/ids/basis for all per-pair launches at once (one region per launch)
+    struct GenLaunch {
+        int kind;          // 0 fixed, 1 spline dataset
+        int d;
+        size_t tile_off, num_tiles, id_off, basis_off;
+    };
+    std::vector<GenLaunch> gl;
+    std::vector<LineTile> all_tiles;
+    std::vector<int> all_ids;
+    std::vector<LineBasis> all_basis;
+    auto add_gen = [&](int kind, int d) {
+        std::vector<int> ids;
+        std::vector<LineTile> tiles;
+        make_tiles(kind == 1 ? &spl[d].mu : nullptr, ids, tiles);
+        GenLaunch g;
+        g.kind = kind;
+        g.d = d;
+        g.tile_off = all_tiles.size();
+        g.num_tiles = tiles.size();
+        g.id_off = all_ids.size();
+        g.basis_off = all_basis.size();
+        for (auto& t : tiles) t.first += (int)g.id_off;
+        all_tiles.insert(all_tiles.end(), tiles.begin(), tiles.end());
+        all_ids.insert(all_ids.end(), ids.begin(), ids.end());
+        if (kind == 1) all_basis.insert(all_basis.end(), spl[d].basis.begin(), spl[d].basis.end());
+        gl.push_back(g);
+    };
+    // generic fixed: when lines do not share an origin (or arc projection is off);
+    // with a shared origin only the near-origin residue goes per pair
+    if (fixed_n_ > 0) add_gen(0, -1);
+    for (size_t d = 0; d < splines_.size(); d++)
+        if (splines_[d].n > 0) add_gen(1, (int)d);
+    gen_tiles_.reserve(std::max<size_t>(1, all_tiles.size()) * sizeof(LineTile));
+    gen_line_ids_.reserve(std::max<size_t>(1, all_ids.size()) * sizeof(int));
+    gen_basis_.reserve(std::max<size_t>(1, all_basis.size()) * sizeof(LineBasis));
+    if (!all_tiles.empty())
+        BCSIM_CUDA(cudaMemcpyAsync(gen_tiles_.get(), all_tiles.data(), all_tiles.size() * sizeof(LineTile), cudaMemcpyHostToDevice, st));
+    if (!all_ids.empty())
+        BCSIM_CUDA(cudaMemcpyAsync(gen_line_ids_.get(), all_ids.data(), all_ids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!all_basis.empty())
+        BCSIM_CUDA(cudaMemcpyAsync(gen_basis_.get(), all_basis.data(), all_basis.size() * sizeof(LineBasis), cudaMemcpyHostToDevice, st));
+
+    // ---------------- shared-origin path ----------------
+    counts_.reserve(4 * sizeof(int));
+    if (n_shared > 0) {
+        timer.restart();
+        const int64_t N = n_shared;
+        keys_in_.reserve(N * sizeof(uint32_t));
+        vals_in_.reserve(N * sizeof(uint32_t));
+        keys_out_.reserve(N * sizeof(uint32_t));
+        vals_out_.reserve(N * sizeof(uint32_t));
+        recA_.reserve(N * sizeof(float4));
+        recB_.reserve(N * sizeof(float4));
+        records_.reserve((size_t)N * 2 * sizeof(float4));
+        const float* origin = lines_[0].o;
+        int64_t off = 0;
+        if (fixed_n_ > 0) {
+            BCSIM_CUDA(launch_prep_shared(fixed_xyza_.as<float4>(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
+                                          vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
+            off = fixed_n_;
+        }
+        std::vector<int64_t> spline_off(splines_.size(), -1);
+        std::vector<double> bd;
+        std::vector<float> bf;
+        for (size_t d = 0; d < splines_.size(); d++) {
+            if (!spline_shared[d]) continue;
+            const SplineDataset& ds = splines_[d];
+            const LineBasis& lb = spl[d].basis[0];
+            bd.clear(); bf.clear();
+            for (int k2 = 0; k2 <= ds.degree; k2++) {
+                bd.push_back((double)lb.hi[k2] + (double)lb.lo[k2]);
+                bf.push_back(lb.hi[k2]);
+            }
+            // exact double basis for the render (the pair above is exact to ~48 bits;
+            // recompute in double for bit parity with the FP64 oracle)
+            if (mode_ == MODE_FP64) {
+                const int lo = spl[d].mu[0] - ds.degree;
+                for (int k2 = 0; k2 <= ds.degree; k2++) bd[k2] = bspline_basis_d(lo + k2, ds.degree, (double)timestamps_[0], ds.knots);
+            }
+            spl_basis_d_.reserve(64 * sizeof(double) * (d + 1));
+            spl_basis_f_.reserve(64 * sizeof(float) * (d + 1));
+            double* bdd = spl_basis_d_.as<double>() + 64 * d;
+            float* bfd = spl_basis_f_.as<float>() + 64 * d;
+            BCSIM_CUDA(cudaMemcpyAsync(bdd, bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+            BCSIM_CUDA(cudaMemcpyAsync(bfd, bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+            BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                                                 spl[d].mu[0] - ds.degree, ds.degree, bdd, bfd, off, origin, p, b,
+                                                 keys_in_.as<uint32_t>(), vals_in_.as<uint32_t>(), recA_.as<float4>(),
+                                                 recB_.as<float4>(), st));
+            BCSIM_CUDA(cudaStreamSynchronize(st));   // bd/bf host vectors are reused
+            spline_off[d] = off;
+            off += ds.n;
+        }
+        int end_bit = 1;
+        while ((1ll << end_bit) < (int64_t)ns + 2) end_bit++;
+        size_t tmp_bytes = 0;
+        BCSIM_CUDA(radix_sort_pairs(nullptr, &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
+                                    vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
+        sort_tmp_.reserve(tmp_bytes);
+        BCSIM_CUDA(radix_sort_pairs(sort_tmp_.get(), &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
+                                    vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
+        BCSIM_CUDA(launch_count_keys(keys_out_.as<uint32_t>(), N, ns, counts_.as<int>(), st));
+        BCSIM_CUDA(launch_gather_records(vals_out_.as<uint32_t>(), counts_.as<int>(), N, recA_.as<float4>(),
+                                         recB_.as<float4>(), records_.as<float4>(), N, st));
+        if (store_details_) debug_["prep_sort_ms"].push_back(timer.stop());
+        timer.restart();
+        // records per CTA: enough CTAs to fill the GPU several times over
+        const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
+        const int64_t groups = (L + threads - 1) / threads;
+        int chunk = 2048;
+        while (chunk > 256 && ((N + chunk - 1) / chunk) * groups < 8 * 152) chunk /= 2;
+        if (tile_lines_ > 0) chunk = std::max(64, std::min(4096, tile_lines_));
+        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, chunk, lines_d, L, p, b, bins, st));
+        // near-origin residue, per pair
+        for (const GenLaunch& g : gl) {
+            if (g.kind == 0) {
+                BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
+                                                  vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
+                                                  gen_line_ids_.as<int>() , gen_tiles_.as<LineTile>() + g.tile_off,
+                                                  (int)g.num_tiles, nullptr, p, b, bins, st));
+            } else if (spline_shared[g.d]) {
+                const SplineDataset& ds = splines_[g.d];
+                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                                                  ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
+                                                  spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
+                                                  gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
+                                                  gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
+            }
+        }
+        if (store_details_) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
+    }
+
+    // ---------------- per-pair path ----------------
+    timer.restart();
+    for (const GenLaunch& g : gl) {
+        if (g.kind == 0) {
+            if (shared) continue;
+            BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
+                                              nullptr, 0, lines_d, gen_line_ids_.as<int>(),
+                                              gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
+                                              b, bins, st));
+        } else {
+            if (spline_shared[g.d]) continue;
+            const SplineDataset& ds = splines_[g.d];
+            BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                                              ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
+                                              gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
+                                              gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
+        }
+    }
+    if (store_details_) debug_[shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
+
+    // ---------------- convolution + demodulation + decimation ----------------
+    timer.restart();
+    BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -S), taps_dev_.as<float2>(),
+                                          (int)tap_count_, (int)tap_start_, M_, center_, decimation_, (int)nd_,
+                                          demod_dev_.as<float2>(), dev_out, st));
+    if (store_details_) debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
+    if (host_out) {
+        timer.restart();
+        BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)L * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
+        BCSIM_CUDA(cudaStreamSynchronize(st));
+        if (store_details_) debug_["kernel_memcpy_ms"].push_back(timer.stop());
+        int flag = 0;
+        BCSIM_CUDA(read_and_clear_error_flag(&flag, st));
+        if (flag) throw SimError(BCSIM_E_INTERNAL, "a bounded device wait gave up; results are incomplete");
+    }
+    if (store_details_) debug_["total_ms"].push_back(total.stop());
+}
+
+void Simulator::simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples) {
+    throw_if_not_configured();
+    int64_t L = 0, nd = 0;
+    output_shape(&L, &nd);
+    if (lines) *lines = L;
+    if (samples) *samples = nd;
+    if (!host_out || cap_complex < L * nd)
+        throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
+    ensure_device();
+    out_.reserve((size_t)L * nd * sizeof(float2));
+    simulate(out_.as<float2>(), host_out);
+}
+
+void Simulator::simulate_device(void* dev_out, int64_t cap_complex) {
+    throw_if_not_configured();
+    int64_t L = 0, nd = 0;
+    output_shape(&L, &nd);
+    if (!dev_out || cap_complex < L * nd)
+        throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
+    simulate(static_cast<float2*>(dev_out), nullptr);
+}
+
+}  // namespace bcsim_gb300

@@ -1,0 +1,166 @@
+// engine.hpp -- the GB300 COLE simulator behind the C ABI.
+//
+// One Simulator mirrors one bcsim::IAlgorithm instance of the reference GPU
+// algorithm (src/core/algorithm/GpuAlgorithm.hpp:48-162): string parameters,
+// excitation, scan sequence, beam profile and scatterer datasets are configured
+// in any order the reference CPU algorithm accepts, scatterers are copied to the
+// device when added and stay resident, and simulate_lines() runs the whole
+// projection -> convolution -> demodulation -> decimation pipeline on one CUDA
+// stream.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "kernels.hpp"
+
+namespace bcsim_gb300 {
+
+// Failure carrying one of the BCSIM_E_* codes and the reference's message.
+struct SimError : public std::runtime_error {
+    int code;
+    SimError(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+// Owning device allocation that only grows.
+class DeviceBuffer {
+public:
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) { o.ptr_ = nullptr; o.bytes_ = 0; }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
+    ~DeviceBuffer();
+    void reserve(size_t bytes);   // grow (contents not kept)
+    void release();
+    void* get() const { return ptr_; }
+    template <typename T> T* as() const { return static_cast<T*>(ptr_); }
+    size_t bytes() const { return bytes_; }
+
+private:
+    void* ptr_ = nullptr;
+    size_t bytes_ = 0;
+};
+
+struct SplineDataset {
+    int degree = 0;
+    int num_cs = 0;
+    std::vector<float> knots;
+    DeviceBuffer cps;      // float4 [num_cs][n] (x, y, z, 0)
+    DeviceBuffer amps;     // float [n]
+    int64_t n = 0;
+    double sum_abs_amp = 0.0;
+};
+
+typedef void (*LogFn)(int level, const char* message, void* user);
+
+class Simulator {
+public:
+    Simulator();
+    ~Simulator();
+
+    void set_parameter(const std::string& key, const std::string& value);
+    std::string get_parameter(const std::string& key) const;
+    void set_excitation(const float* samples, int n, int center_index, float fs, float demod_freq);
+    void set_scan_sequence(const float* origins, const float* dirs, const float* lats, const float* timestamps,
+                           int num_lines, float line_length);
+    void set_analytical_profile(float sigma_lateral, float sigma_elevational);
+    void set_lookup_profile(const float* samples, int nr, int nl, int ne, float r0, float r1, float l0, float l1,
+                            float e0, float e1);
+    void clear_fixed_scatterers();
+    void add_fixed_scatterers(const float* xyza, int64_t n);
+    void clear_spline_scatterers();
+    void add_spline_scatterers(int degree, const float* knots, int num_knots, const float* cps, const float* amps,
+                               int64_t n, int num_cs);
+    int64_t total_num_scatterers() const;
+    void output_shape(int64_t* lines, int64_t* samples) const;
+
+    // Runs the pipeline into device memory dev_out (complex64 [L][nd]); if
+    // host_out is given, also copies to it and synchronises.
+    void simulate(float2* dev_out, float* host_out);
+    void simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples);
+    void simulate_device(void* dev_out, int64_t cap_complex);
+
+    std::vector<double> get_debug_data(const std::string& key) const;
+    void set_logger(LogFn fn, void* user) { log_fn_ = fn; log_user_ = user; }
+    cudaStream_t stream();
+
+private:
+    void log(int level, const std::string& msg) const;
+    void ensure_device();
+    void throw_if_not_configured() const;
+    void prepare_excitation_tables();
+    void prepare_lines();
+    double fixed_point_bound() const;
+
+    // configuration
+    int device_ = 0;
+    bool device_ready_ = false;
+    cudaStream_t stream_ = nullptr;
+    int verbose_ = 0;
+    float sound_speed_ = 1540.0f;
+    float noise_amplitude_ = 0.0f;
+    bool arc_ = true;
+    int decimation_ = 1;
+    bool phase_delay_ = false;
+    int cuda_streams_ = 2;
+    int threads_per_block_ = 128;
+    bool store_details_ = false;
+    int mode_ = MODE_FP64;
+    double fir_tail_ = 1e-10;
+    int tile_lines_ = 0;   // 0 = automatic
+
+    bool excitation_set_ = false;
+    std::vector<float> taps_;
+    int center_ = 0;
+    float fs_ = 0.0f, fd_ = 0.0f;
+
+    bool scan_set_ = false;
+    int num_lines_ = 0;
+    float line_length_ = 0.0f;
+    int64_t ns_ = 0;
+    std::vector<LineGeom> lines_;
+    std::vector<float> timestamps_;
+    bool shared_origin_ = false;
+    bool timestamps_equal_ = false;
+
+    int beam_type_ = 0;   // 0 = not configured
+    float sigma_l_ = 0.0f, sigma_e_ = 0.0f;
+    std::vector<float> lut_;
+    int lut_nr_ = 0, lut_nl_ = 0, lut_ne_ = 0;
+    float lut_ext_[6] = {0, 0, 0, 0, 0, 0};
+    double lut_absmax_ = 0.0;
+    DeviceBuffer lut4_;
+    bool lut_uploaded_ = false;
+
+    // all fixed datasets, appended into one float4 [n] array (x, y, z, a)
+    DeviceBuffer fixed_xyza_;
+    int64_t fixed_n_ = 0;
+    int num_fixed_sets_ = 0;
+    double fixed_sum_abs_ = 0.0;
+    bool amplitude_nonfinite_ = false;
+    std::vector<SplineDataset> splines_;
+
+    // derived device state
+    bool tables_valid_ = false;
+    int64_t M_ = 0, nd_ = 0;
+    int64_t tap_start_ = 0, tap_count_ = 0;
+    DeviceBuffer taps_dev_, demod_dev_;
+    bool lines_valid_ = false;
+    DeviceBuffer lines_dev_;
+    DeviceBuffer bins_, out_;
+    DeviceBuffer keys_in_, vals_in_, keys_out_, vals_out_, recA_, recB_, records_, sort_tmp_, counts_;
+    DeviceBuffer gen_tiles_, gen_line_ids_, gen_basis_, spl_basis_d_, spl_basis_f_;
+    std::vector<float> pinned_dummy_;
+
+    std::map<std::string, std::vector<double>> debug_;
+    LogFn log_fn_ = nullptr;
+    void* log_user_ = nullptr;
+};
+
+}  // namespace bcsim_gb300

@@ -1,0 +1,137 @@
+// kernels.hpp -- structures shared by the host engine and the CUDA kernels, and
+// the host-side launchers of every kernel.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bcsim_gb300 {
+
+// One scan line as the kernels see it: origin, radial, lateral and elevational
+// unit vectors (elevational = lateral x radial, computed on the host in float as
+// src/core/ScanSequence.cpp:40 does).
+struct LineGeom {
+    float o[3];
+    float d[3];
+    float l[3];
+    float e[3];
+};
+
+enum BeamType : int { BEAM_GAUSSIAN = 1, BEAM_LUT = 2 };
+enum PrecisionMode : int { MODE_FP64 = 0, MODE_REFERENCE = 1 };
+
+// Beam profile constants.
+struct BeamDev {
+    int type;
+    // Gaussian, fp64 mode: w = exp2(-(l^2 * gl + e^2 * ge)), gl = log2(e) / (2 sigma_l^2)
+    float gl, ge;
+    // Gaussian, reference mode: w = expf(-(l*l/two_sl2 + e*e/two_se2)) (BeamProfile.cpp:49-56)
+    float two_sl2, two_se2;
+    // Lookup table: packed corners, see pack_lut() in engine.cpp
+    const float4* lut4;
+    int nr, nl, ne;
+    float rf, lf, ef;          // first sample positions
+    float inv_dr, inv_dl, inv_de;  // 1 / spacing (fp64 mode, per-pair coordinates)
+    double dr, dl, de;         // spacing as the mode defines it (double)
+};
+
+// Constants of one simulation.
+struct SimParams {
+    int ns;                    // time samples per line (before decimation)
+    int num_lines;
+    int phase_delay;
+    int arc;
+    int mode;                  // PrecisionMode
+    float fs, c, fd;
+    double fs_d, c_d, fd_d;
+    float k_hi, k_lo;          // 2 fs / c as a float pair (fp64 generic path)
+    float two_pi_fd_over_fs;   // phase per sample of sub-sample delay
+    float scale;               // fixed-point scale 2^S for bin accumulation
+    int log2scale;
+};
+
+// A tile of lines for the per-pair projection kernel: `count` lines taken from
+// line_ids[first ...], all sharing the spline knot interval `mu`.
+struct LineTile {
+    int first;
+    int count;
+    int mu;
+    int pad;
+};
+
+// Per-line spline basis: p+1 non-zero basis values as float pairs (hi, lo),
+// starting at control point mu - degree.
+constexpr int MAX_SPLINE_DEGREE = 7;
+struct LineBasis {
+    float hi[MAX_SPLINE_DEGREE + 1];
+    float lo[MAX_SPLINE_DEGREE + 1];
+};
+
+// Shared-origin records, in bin order, as two planes of float4:
+//   A = (dx, dy, dz, amplitude * cos(phase))   relative to the common origin
+//   B = (amplitude * sin(phase), radial LUT fraction, radial LUT index bits, bin bits)
+
+// ---------------------------------------------------------------------------
+// launchers (all asynchronous on `stream`; return cudaGetLastError())
+// ---------------------------------------------------------------------------
+
+// Per scatterer, from a shared line origin: exact bin index (fp64 or reference
+// arithmetic), phase-rotated amplitude and LUT radial coordinate.  Writes sort
+// keys (bin index, or ns for near-origin scatterers that need the per-pair path,
+// or ns+1 for scatterers that no line can see), identity values and the
+// unsorted records.
+cudaError_t launch_prep_shared(const float4* xyza, int64_t n, int64_t out_offset, const float origin[3],
+                               const SimParams& p, const BeamDev& b, uint32_t* keys, uint32_t* vals,
+                               float4* recA, float4* recB, cudaStream_t stream);
+
+// Same, for spline scatterers evaluated at one common timestamp in double.
+cudaError_t launch_prep_shared_spline(const float4* cps, const float* amps, int64_t n, int num_cs, int first_cs,
+                                      int degree, const double* basis_d, const float* basis_f,
+                                      int64_t out_offset, const float origin[3], const SimParams& p,
+                                      const BeamDev& b, uint32_t* keys, uint32_t* vals, float4* recA,
+                                      float4* recB, cudaStream_t stream);
+
+// Sorted keys -> counts: counts[0] = #keys < ns, counts[1] = #keys == ns
+// (counts needs 4 ints).
+cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int* counts, cudaStream_t stream);
+
+// Sorted values -> record planes in bin order (plane B starts at out + plane).
+cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts, int64_t n, const float4* recA,
+                                  const float4* recB, float4* out, int64_t plane, cudaStream_t stream);
+
+// Projection of the counts[0] sorted records onto all lines (lines share the
+// origin); `chunk` records per CTA, one line per thread.
+cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
+                                  const LineGeom* lines, int num_lines, const SimParams& p, const BeamDev& b,
+                                  unsigned long long* bins, cudaStream_t stream);
+
+// Per-pair projection: fixed scatterers (cps == nullptr) or splines, arbitrary
+// lines.  If index_list is given, the entries index_list[counts[0] ...
+// counts[0]+counts[1]) that fall in [list_lo, list_lo + n) are projected, as
+// scatterer (entry - list_lo) -- the near-origin residue of the shared path;
+// otherwise scatterers [0, n).
+cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const float* amps, int64_t n,
+                                   int num_cs, int degree, const uint32_t* index_list, const int* counts,
+                                   int64_t list_lo,
+                                   const LineGeom* lines, const int* line_ids, const LineTile* tiles,
+                                   int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
+                                   unsigned long long* bins, cudaStream_t stream);
+
+// Fused convolution with the analytic pulse (direct FIR over a tap window),
+// IQ demodulation and radial decimation, from fixed-point bins to complex64.
+cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
+                                       float inv_scale, const float2* taps, int num_taps, int tap_start,
+                                       int64_t M, int center, int decimation, int nd, const float2* demod,
+                                       float2* out, cudaStream_t stream);
+
+// Radix sort of (key, value) pairs: key bits [0, end_bit).  temp == nullptr
+// queries the scratch size into *temp_bytes.
+cudaError_t radix_sort_pairs(void* temp, size_t* temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,
+                             const uint32_t* vals_in, uint32_t* vals_out, int64_t n, int end_bit,
+                             cudaStream_t stream);
+
+}  // namespace bcsim_gb300
+
+namespace bcsim_gb300 {
+// Reads and clears the device flag that a bounded wait sets when it gives up.
+cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream);
+}

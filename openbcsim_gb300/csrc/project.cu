@@ -1,0 +1,752 @@
+// project.cu -- scatterer -> scan-line time projection on sm_103a.
+//
+// Semantics follow the reference CPU projection loops
+// (src/core/algorithm/CpuAlgorithm.cpp:50-183): for every (scatterer, line)
+// pair the scatterer is expressed in the line's frame (r, l, e), the radial
+// coordinate is replaced by the signed distance to the origin when arc
+// projection is on, the bin index is floor(r * 2 fs / c + 0.5), the beam weight
+// is the Gaussian of src/core/BeamProfile.cpp:49-51 or the trilinear lookup of
+// src/core/BeamProfile.cpp:79-130, and (optionally) the sub-sample delay is
+// applied as a phase (CpuAlgorithm.cpp:85-95).
+//
+// Two paths:
+//  * shared origin (every line starts at the same point, arc projection on):
+//    the distance to the origin -- and therefore the bin index and the phase --
+//    does not depend on the line.  prep computes them once per scatterer in FP64
+//    (bit-identical to the FP64 oracle's expression), the records are radix
+//    sorted by bin, and the projection kernel walks runs of equal bins with the
+//    line frame in registers, summing in FP32 registers and flushing each run
+//    once per line into fixed-point bins.
+//  * per pair (any geometry, splines): the time of flight is computed per pair
+//    with float-pair arithmetic, each non-zero contribution goes to the bins.
+//
+// Bins are signed 64-bit fixed point (value * 2^S); integer addition is
+// associative, so the result does not depend on the order in which CTAs,
+// warps or atomics land: the accumulation is deterministic by construction,
+// where the reference's GPU path (cuda_kernels_fixed.cuh:59-62) uses float
+// atomics whose order varies from run to run.
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cub/device/device_radix_sort.cuh>
+#include "kernels.hpp"
+#include "dfloat.cuh"
+
+namespace bcsim_gb300 {
+
+static constexpr double TWO_PI_LITERAL = 6.283185307179586;  // CpuAlgorithm.cpp:89,175
+
+// ---------------------------------------------------------------------------
+// fixed-point accumulation
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bin_add(unsigned long long* addr, float v, float scale) {
+    if (v != 0.0f) {
+        const long long q = __float2ll_rn(v * scale);
+        if (q != 0) atomicAdd(addr, (unsigned long long)q);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Lookup-table weight shared by both paths, float arithmetic, given the radial
+// table coordinate (r0, fr) and the lateral/elevational positions.
+// The packed table holds, at (r, l, e), the corners
+// (c[r][l][e], c[r][l][e+1], c[r+1][l][e], c[r+1][l][e+1]).
+// Valid coordinate range per axis is -1 < t < n-1 (the reference's index test
+// for trunc-toward-zero indices, BeamProfile.cpp:94-103); for -1 < t < 0 both
+// indices are 0 and the fraction is dropped.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float lut_weight_packed(const BeamDev& b, int r0, float fr, float tl, float te) {
+    if (!(tl > -1.0f && tl < (float)(b.nl - 1) && te > -1.0f && te < (float)(b.ne - 1))) return 0.0f;
+    const int l0 = (int)tl, e0 = (int)te;
+    const float fl = tl < 0.0f ? 0.0f : tl - (float)l0;
+    const float fe = te < 0.0f ? 0.0f : te - (float)e0;
+    const int base = (r0 * b.nl + l0) * b.ne + e0;
+    const float4 P = __ldg(b.lut4 + base);            // (r0,l0,e0) (r0,l0,e1) (r1,l0,e0) (r1,l0,e1)
+    const float4 Q = __ldg(b.lut4 + base + b.ne);     // same at l1
+    // radial, then lateral, then elevational interpolation (BeamProfile.cpp:116-127)
+    const float c00 = __fmaf_rn(fr, P.z - P.x, P.x);
+    const float c01 = __fmaf_rn(fr, P.w - P.y, P.y);
+    const float c10 = __fmaf_rn(fr, Q.z - Q.x, Q.x);
+    const float c11 = __fmaf_rn(fr, Q.w - Q.y, Q.y);
+    const float c0 = __fmaf_rn(fl, c10 - c00, c00);
+    const float c1 = __fmaf_rn(fl, c11 - c01, c01);
+    return __fmaf_rn(fe, c1 - c0, c0);
+}
+
+// Lookup-table weight in the reference's own arithmetic (reference mode,
+// BeamProfile.cpp:79-130): float differences divided by double spacings,
+// trunc indices, float interpolation weights.
+__device__ float lut_weight_ref(const BeamDev& b, float r, float l, float e) {
+    const double tr = (double)__fsub_rn(r, b.rf) / b.dr;
+    const double tl = (double)__fsub_rn(l, b.lf) / b.dl;
+    const double te = (double)__fsub_rn(e, b.ef) / b.de;
+    if (!(tr > -1.0 && tr < (double)(b.nr - 1))) return 0.0f;
+    if (!(tl > -1.0 && tl < (double)(b.nl - 1))) return 0.0f;
+    if (!(te > -1.0 && te < (double)(b.ne - 1))) return 0.0f;
+    const int r0 = (int)tr, l0 = (int)tl, e0 = (int)te;
+    const float fr = tr < 0.0 ? 0.0f : (float)(tr - r0);
+    const float fl = tl < 0.0 ? 0.0f : (float)(tl - l0);
+    const float fe = te < 0.0 ? 0.0f : (float)(te - e0);
+    const int base = (r0 * b.nl + l0) * b.ne + e0;
+    const float4 P = __ldg(b.lut4 + base);
+    const float4 Q = __ldg(b.lut4 + base + b.ne);
+    const float omr = __fsub_rn(1.0f, fr), oml = __fsub_rn(1.0f, fl), ome = __fsub_rn(1.0f, fe);
+    const float c00 = __fadd_rn(__fmul_rn(omr, P.x), __fmul_rn(fr, P.z));
+    const float c10 = __fadd_rn(__fmul_rn(omr, Q.x), __fmul_rn(fr, Q.z));
+    const float c01 = __fadd_rn(__fmul_rn(omr, P.y), __fmul_rn(fr, P.w));
+    const float c11 = __fadd_rn(__fmul_rn(omr, Q.y), __fmul_rn(fr, Q.w));
+    const float c0 = __fadd_rn(__fmul_rn(oml, c00), __fmul_rn(fl, c10));
+    const float c1 = __fadd_rn(__fmul_rn(oml, c01), __fmul_rn(fl, c11));
+    return __fadd_rn(__fmul_rn(ome, c0), __fmul_rn(fe, c1));
+}
+
+// Gaussian weight in the reference's arithmetic (BeamProfile.cpp:49-56).
+__device__ __forceinline__ float gauss_weight_ref(const BeamDev& b, float l, float e) {
+    const float q = __fadd_rn(__fdiv_rn(__fmul_rn(l, l), b.two_sl2), __fdiv_rn(__fmul_rn(e, e), b.two_se2));
+    return expf(-q);
+}
+
+// ---------------------------------------------------------------------------
+// shared-origin prep
+// ---------------------------------------------------------------------------
+struct PrepOut {
+    uint32_t key;
+    float4 A, B;
+};
+
+// dx,dy,dz: the scatterer relative to the origin in double (fp64 mode) and as
+// the reference's float subtraction (reference mode); a: amplitude.
+// spline selects the spline loop's index expression r*2/(c*dt), dt = 1/fs
+// (CpuAlgorithm.cpp:161-162), over the fixed loop's r*2*fs/c (:75).
+__device__ __forceinline__ PrepOut prep_one(double dx, double dy, double dz, float fdx, float fdy, float fdz,
+                                            float a, const SimParams& p, const BeamDev& b, bool spline) {
+    PrepOut o;
+    double rho, t;
+    if (p.mode == MODE_FP64) {
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        rho = __dsqrt_rn(r2);
+    } else {
+        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), __fmul_rn(fdz, fdz));
+        rho = (double)__fsqrt_rn(r2);
+    }
+    if (!spline) {
+        // t = r * 2.0 * fs / c, evaluated left to right as CpuAlgorithm.cpp:75
+        t = __ddiv_rn(__dmul_rn(__dmul_rn(rho, 2.0), p.fs_d), p.c_d);
+    } else if (p.mode == MODE_FP64) {
+        t = __ddiv_rn(__dmul_rn(rho, 2.0), __dmul_rn(p.c_d, __ddiv_rn(1.0, p.fs_d)));
+    } else {
+        const float dt = (float)(1.0 / p.fs_d);
+        t = __ddiv_rn(__dmul_rn(rho, 2.0), (double)__fmul_rn(p.c, dt));
+    }
+    const double fidx = floor(t + 0.5);
+    uint32_t key;
+    if (!(t == t) || !(fidx < (double)p.ns)) {
+        key = (uint32_t)p.ns + 1u;               // beyond the line end for every line
+    } else if (t <= 0.5) {
+        key = (uint32_t)p.ns;                    // near origin: a line behind may still hit bin 0
+    } else {
+        key = (uint32_t)fidx;
+    }
+    const int idx = (int)fidx;
+    float Ar = a, Ai = 0.0f;
+    if (p.phase_delay && key < (uint32_t)p.ns) {
+        if (p.mode == MODE_FP64) {
+            const double delay = ((double)idx - t) / p.fs_d;
+            const double ph = TWO_PI_LITERAL * p.fd_d * delay;
+            double s, c;
+            sincos(ph, &s, &c);
+            Ar = (float)((double)a * c);
+            Ai = (float)((double)a * s);
+        } else {
+            const float ss_delay = (float)(((double)idx - t) / p.fs_d);
+            const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
+            float s, c;
+            sincosf(ph, &s, &c);
+            Ar = __fmul_rn(a, c);
+            Ai = __fmul_rn(a, s);
+        }
+    }
+    int r0 = 0;
+    float fr = 0.0f;
+    if (b.type == BEAM_LUT && key < (uint32_t)p.ns) {
+        double tr;
+        if (p.mode == MODE_FP64) tr = (rho - (double)b.rf) / b.dr;
+        else tr = (double)__fsub_rn((float)rho, b.rf) / b.dr;
+        if (!(tr > -1.0 && tr < (double)(b.nr - 1))) {
+            key = (uint32_t)p.ns + 1u;           // radial coordinate outside the table: weight 0
+        } else {
+            r0 = (int)tr;
+            fr = tr < 0.0 ? 0.0f : (float)(tr - (double)r0);
+        }
+    }
+    o.key = key;
+    o.A = make_float4(fdx, fdy, fdz, Ar);
+    o.B = make_float4(Ai, fr, __int_as_float(r0), __int_as_float(idx));
+    return o;
+}
+
+__global__ void prep_shared_kernel(const float4* __restrict__ xyza, int64_t n, int64_t off, double ox, double oy,
+                                   double oz, float ofx, float ofy, float ofz, SimParams p, BeamDev b,
+                                   uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                   float4* __restrict__ recA, float4* __restrict__ recB) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = __ldg(xyza + i);
+    const double dx = __dsub_rn((double)q.x, ox), dy = __dsub_rn((double)q.y, oy), dz = __dsub_rn((double)q.z, oz);
+    const float fdx = __fsub_rn(q.x, ofx), fdy = __fsub_rn(q.y, ofy), fdz = __fsub_rn(q.z, ofz);
+    const PrepOut o = prep_one(dx, dy, dz, fdx, fdy, fdz, q.w, p, b, false);
+    keys[off + i] = o.key;
+    vals[off + i] = (uint32_t)(off + i);
+    recA[off + i] = o.A;
+    recB[off + i] = o.B;
+}
+
+// Spline scatterers at one common timestamp: position = sum_i B_i * C_i over the
+// degree+1 non-zero basis functions, in double (fp64 mode) or in the reference's
+// float accumulation (reference mode, CpuAlgorithm.cpp:137-140).
+__global__ void prep_shared_spline_kernel(const float4* __restrict__ cps, const float* __restrict__ amps, int64_t n,
+                                          int first_cs, int degree, const double* __restrict__ bd,
+                                          const float* __restrict__ bf, int64_t off, double ox, double oy,
+                                          double oz, float ofx, float ofy, float ofz, SimParams p, BeamDev b,
+                                          uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                          float4* __restrict__ recA, float4* __restrict__ recB) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double px = 0.0, py = 0.0, pz = 0.0;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    for (int k = 0; k <= degree; k++) {
+        const float4 c = __ldg(cps + (int64_t)(first_cs + k) * n + i);
+        if (p.mode == MODE_FP64) {
+            px = __dadd_rn(px, __dmul_rn((double)c.x, bd[k]));
+            py = __dadd_rn(py, __dmul_rn((double)c.y, bd[k]));
+            pz = __dadd_rn(pz, __dmul_rn((double)c.z, bd[k]));
+        } else {
+            fx = __fadd_rn(fx, __fmul_rn(c.x, bf[k]));
+            fy = __fadd_rn(fy, __fmul_rn(c.y, bf[k]));
+            fz = __fadd_rn(fz, __fmul_rn(c.z, bf[k]));
+        }
+    }
+    double dx, dy, dz;
+    float fdx, fdy, fdz;
+    if (p.mode == MODE_FP64) {
+        dx = __dsub_rn(px, ox); dy = __dsub_rn(py, oy); dz = __dsub_rn(pz, oz);
+        fdx = (float)dx; fdy = (float)dy; fdz = (float)dz;
+    } else {
+        fdx = __fsub_rn(fx, ofx); fdy = __fsub_rn(fy, ofy); fdz = __fsub_rn(fz, ofz);
+        dx = fdx; dy = fdy; dz = fdz;
+    }
+    const PrepOut o = prep_one(dx, dy, dz, fdx, fdy, fdz, __ldg(amps + i), p, b, true);
+    keys[off + i] = o.key;
+    vals[off + i] = (uint32_t)(off + i);
+    recA[off + i] = o.A;
+    recB[off + i] = o.B;
+}
+
+// Boundaries of the sorted keys: counts[2] = first index with key >= ns,
+// counts[3] = first index with key > ns (both n if absent).
+__global__ void init_counts_kernel(int* counts, int64_t n) {
+    counts[0] = 0;
+    counts[1] = 0;
+    counts[2] = (int)n;
+    counts[3] = (int)n;
+}
+
+__global__ void count_keys_kernel(const uint32_t* __restrict__ keys, int64_t n, int ns, int* counts) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = keys[i];
+    const bool first = i == 0;
+    const uint32_t prev = first ? 0u : keys[i - 1];
+    if (k >= (uint32_t)ns && (first || prev < (uint32_t)ns)) counts[2] = (int)i;
+    if (k > (uint32_t)ns && (first || prev <= (uint32_t)ns)) counts[3] = (int)i;
+}
+
+// counts[0] = #keys < ns (records for the shared-origin kernel),
+// counts[1] = #keys == ns (near-origin scatterers for the per-pair kernel).
+__global__ void finish_counts_kernel(int* counts) {
+    counts[0] = counts[2];
+    counts[1] = counts[3] - counts[2];
+}
+
+// Sorted values -> the two record planes in bin order (plane B at out + plane).
+__global__ void gather_records_kernel(const uint32_t* __restrict__ svals, const int* __restrict__ counts,
+                                      int64_t n, const float4* __restrict__ recA, const float4* __restrict__ recB,
+                                      float4* __restrict__ out, int64_t plane) {
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || s >= (int64_t)__ldg(counts)) return;
+    const uint32_t src = svals[s];
+    out[s] = recA[src];
+    out[plane + s] = recB[src];
+}
+
+// ---------------------------------------------------------------------------
+// shared-origin projection
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+// Wait for phase `parity` of the barrier, giving up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    for (unsigned it = 0; it < limit; it++) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+}
+
+// 1-D TMA bulk copy global -> shared, completion counted on `bar`.
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, unsigned bytes, uint64_t* bar) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+                 "l"(gsrc), "r"(bytes), "r"(b)
+                 : "memory");
+}
+
+__device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
+
+// Records per folding of the FP32 run sum into the integer bin total: bounds
+// the length of any FP32 summation to FOLD terms.
+constexpr int FOLD = 128;
+
+// One CTA: a chunk of `chunk` consecutive records (sorted by bin) x one line
+// per thread.  Every thread walks the same records in the same order (records
+// are broadcast from shared memory, the bin-change branch is warp-uniform),
+// sums its line's contributions of a bin in FP32, folds into an int64 total
+// every FOLD records and writes the bin when the bin changes: with a plain
+// store for bins that lie strictly inside the chunk (no other CTA has records
+// there), with an integer atomic for the chunk's first and last bin.
+template <bool PD, int BEAM, bool REF>
+__global__ void __launch_bounds__(256)
+    project_shared_kernel(const float4* __restrict__ records, int64_t plane, const int* __restrict__ counts, int chunk,
+                          const LineGeom* __restrict__ lines, int L, unsigned long long* __restrict__ bins,
+                          SimParams p, BeamDev b) {
+    extern __shared__ __align__(128) float4 sm[];
+    __shared__ __align__(8) uint64_t bar;
+    const int n_valid = __ldg(counts);
+    const int64_t start = (int64_t)blockIdx.x * chunk;
+    if (start >= n_valid) return;
+    const int cnt = (int)min((int64_t)chunk, (int64_t)n_valid - start);
+    const int tid = threadIdx.x;
+    float4* smA = sm;
+    float4* smB = sm + chunk;
+
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned bytes = (unsigned)cnt * sizeof(float4);
+        mbar_expect_tx(&bar, 2 * bytes);
+        bulk_load(smA, records + start, bytes, &bar);
+        bulk_load(smB, records + plane + start, bytes, &bar);
+    }
+    const int line = blockIdx.y * blockDim.x + tid;
+    const bool active = line < L;
+    const LineGeom* g = lines + (active ? line : L - 1);
+    const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
+    const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
+    const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
+    if (!mbar_wait(&bar, 0, 1u << 26)) {
+        g_bcsim_error_flag = 1;
+        mbar_wait(&bar, 0, 1u << 26);
+        return;
+    }
+
+    const int stride = PD ? 2 : 1;
+    unsigned long long* lbins = bins + (int64_t)(active ? line : 0) * p.ns * stride;
+    const float scale = p.scale;
+    const int first_bin = __float_as_int(smB[0].w);
+    const int last_bin = __float_as_int(smB[cnt - 1].w);
+    int cur = first_bin;
+    long long tot_r = 0, tot_i = 0;
+    float ar = 0.0f, ai = 0.0f;
+    int since_fold = 0;
+
+    for (int i = 0; i < cnt; i++) {
+        const float4 B = smB[i];
+        const int idx = __float_as_int(B.w);
+        if (idx != cur) {
+            tot_r += __float2ll_rn(ar * scale);
+            if (PD) tot_i += __float2ll_rn(ai * scale);
+            if (active) {
+                if (cur == first_bin || cur == last_bin) {
+                    if (tot_r) atomicAdd(lbins + (int64_t)cur * stride, (unsigned long long)tot_r);
+                    if (PD && tot_i) atomicAdd(lbins + (int64_t)cur * stride + 1, (unsigned long long)tot_i);
+                } else {
+                    if (tot_r) lbins[(int64_t)cur * stride] = (unsigned long long)tot_r;
+                    if (PD && tot_i) lbins[(int64_t)cur * stride + 1] = (unsigned long long)tot_i;
+                }
+            }
+            cur = idx;
+            tot_r = tot_i = 0;
+            ar = ai = 0.0f;
+            since_fold = 0;
+        } else if (since_fold == FOLD) {
+            tot_r += __float2ll_rn(ar * scale);
+            if (PD) tot_i += __float2ll_rn(ai * scale);
+            ar = ai = 0.0f;
+            since_fold = 0;
+        }
+        since_fold++;
+        const float4 A = smA[i];
+        float l, e, dot;
+        if (REF) {
+            // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
+            dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, rx), __fmul_rn(A.y, ry)), __fmul_rn(A.z, rz));
+            l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, lx), __fmul_rn(A.y, ly)), __fmul_rn(A.z, lz));
+            e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, ex), __fmul_rn(A.y, ey)), __fmul_rn(A.z, ez));
+        } else {
+            dot = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
+            l = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
+            e = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
+        }
+        float w;
+        if (BEAM == BEAM_GAUSSIAN) {
+            if (REF) w = gauss_weight_ref(b, l, e);
+            else w = exp2f(-fmaf(l * l, b.gl, e * e * b.ge));
+        } else {
+            if (REF) {
+                // the reference recomputes the radial table coordinate per pair from r
+                w = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                          __fmul_rn(A.z, A.z))),
+                                   l, e);
+            } else {
+                const float tl = (l - b.lf) * b.inv_dl;
+                const float te = (e - b.ef) * b.inv_de;
+                w = lut_weight_packed(b, __float_as_int(B.z), B.y, tl, te);
+            }
+        }
+        // arc projection: a line for which the scatterer lies behind the origin
+        // sees it at -rho, outside [0, ns) for every record (near-origin
+        // scatterers take the per-pair path)
+        w = signbit(dot) ? 0.0f : w;
+        ar = fmaf(w, A.w, ar);
+        if (PD) ai = fmaf(w, B.x, ai);
+    }
+    tot_r += __float2ll_rn(ar * scale);
+    if (PD) tot_i += __float2ll_rn(ai * scale);
+    if (active) {
+        if (cur == first_bin || cur == last_bin) {
+            if (tot_r) atomicAdd(lbins + (int64_t)cur * stride, (unsigned long long)tot_r);
+            if (PD && tot_i) atomicAdd(lbins + (int64_t)cur * stride + 1, (unsigned long long)tot_i);
+        } else {
+            if (tot_r) lbins[(int64_t)cur * stride] = (unsigned long long)tot_r;
+            if (PD && tot_i) lbins[(int64_t)cur * stride + 1] = (unsigned long long)tot_i;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-pair projection
+// ---------------------------------------------------------------------------
+constexpr int GENERIC_THREADS = 256;
+
+template <int BEAM, bool SPLINE, bool REF>
+__global__ void __launch_bounds__(GENERIC_THREADS)
+    project_generic_kernel(const float4* __restrict__ xyza, const float4* __restrict__ cps,
+                           const float* __restrict__ amps, int64_t n, int degree,
+                           const uint32_t* __restrict__ index_list, const int* __restrict__ counts,
+                           int64_t list_lo, const LineGeom* __restrict__ lines, const int* __restrict__ line_ids,
+                           const LineTile* __restrict__ tiles, const LineBasis* __restrict__ basis,
+                           unsigned long long* __restrict__ bins, SimParams p, BeamDev b) {
+    const LineTile tile = tiles[blockIdx.y];
+    int64_t count = n;
+    int64_t list_off = 0;
+    if (index_list) {
+        list_off = __ldg(counts);
+        count = __ldg(counts + 1);
+    }
+    const int stride = p.phase_delay ? 2 : 1;
+    for (int64_t s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s0 < count;
+         s0 += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = s0;
+        if (index_list) {
+            s = (int64_t)__ldg(index_list + list_off + s0) - list_lo;
+            if (s < 0 || s >= n) continue;
+        }
+        float a;
+        float4 c[MAX_SPLINE_DEGREE + 1];
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (SPLINE) {
+            a = __ldg(amps + s);
+#pragma unroll
+            for (int k = 0; k <= MAX_SPLINE_DEGREE; k++)
+                if (k <= degree) c[k] = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+        } else {
+            const float4 q = __ldg(xyza + s);
+            px = q.x; py = q.y; pz = q.z; a = q.w;
+        }
+        for (int j = 0; j < tile.count; j++) {
+            const int line = __ldg(line_ids + tile.first + j);
+            const LineGeom* g = lines + line;
+            const float ox = __ldg(&g->o[0]), oy = __ldg(&g->o[1]), oz = __ldg(&g->o[2]);
+            const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
+            const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
+            const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
+            float w, cph = 1.0f, sph = 0.0f;
+            int idx;
+            if (!REF) {
+                // position relative to the origin as float pairs
+                df dx, dy, dz;
+                if (SPLINE) {
+                    const LineBasis* lb = basis + line;
+                    df sx = df_make(0.f, 0.f), sy = df_make(0.f, 0.f), sz = df_make(0.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                        if (k <= degree) {
+                            const df bk = df_make(__ldg(&lb->hi[k]), __ldg(&lb->lo[k]));
+                            sx = df_add(sx, df_mul_f(bk, c[k].x));
+                            sy = df_add(sy, df_mul_f(bk, c[k].y));
+                            sz = df_add(sz, df_mul_f(bk, c[k].z));
+                        }
+                    }
+                    dx = df_add(sx, df_make(-ox, 0.f));
+                    dy = df_add(sy, df_make(-oy, 0.f));
+                    dz = df_add(sz, df_make(-oz, 0.f));
+                } else {
+                    dx = df_diff_f(px, ox);
+                    dy = df_diff_f(py, oy);
+                    dz = df_diff_f(pz, oz);
+                }
+                const float fx = dx.hi + dx.lo, fy = dy.hi + dy.lo, fz = dz.hi + dz.lo;
+                const float dot = fmaf(fz, rz, fmaf(fy, ry, fx * rx));
+                const float l = fmaf(fz, lz, fmaf(fy, ly, fx * lx));
+                const float e = fmaf(fz, ez, fmaf(fy, ey, fx * ex));
+                df r;
+                if (p.arc) {
+                    const df r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
+                    r = df_sqrt(r2);
+                    if (signbit(dot)) { r.hi = -r.hi; r.lo = -r.lo; }
+                } else {
+                    r = df_add(df_add(df_mul_f(dx, rx), df_mul_f(dy, ry)), df_mul_f(dz, rz));
+                }
+                const df t = df_mul(r, df_make(p.k_hi, p.k_lo));
+                // idx = floor(t + 0.5) decided on the pair value: with f = floor(hi)
+                // the remainder hi - f is exact, so compare (hi - f - 0.5) with -lo.
+                float f = floorf(t.hi);
+                float rem = t.hi - f;                   // exact
+                float frac_lo = t.lo;
+                if (rem + frac_lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
+                const bool up = (rem - 0.5f) >= -frac_lo;
+                const float fidx = up ? f + 1.0f : f;
+                if (!(fidx >= 0.0f && fidx < (float)p.ns)) continue;
+                idx = (int)fidx;
+                if (BEAM == BEAM_GAUSSIAN) {
+                    w = exp2f(-fmaf(l * l, b.gl, e * e * b.ge));
+                } else {
+                    const float rr = r.hi + r.lo;
+                    const float tr = (rr - b.rf) * b.inv_dr;
+                    if (!(tr > -1.0f && tr < (float)(b.nr - 1))) continue;
+                    const int r0 = (int)tr;
+                    const float frr = tr < 0.0f ? 0.0f : tr - (float)r0;
+                    w = lut_weight_packed(b, r0, frr, (l - b.lf) * b.inv_dl, (e - b.ef) * b.inv_de);
+                }
+                if (p.phase_delay) {
+                    // sub-sample delay (idx - t) in samples, as a phase (CpuAlgorithm.cpp:85-92)
+                    const float dly = (up ? 1.0f : 0.0f) - rem - frac_lo;
+                    sincosf(p.two_pi_fd_over_fs * dly, &sph, &cph);
+                }
+            } else {
+                // the reference's float expressions (CpuAlgorithm.cpp:58-95 and 137-181)
+                float fx, fy, fz;
+                if (SPLINE) {
+                    const LineBasis* lb = basis + line;
+                    float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                    for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                        if (k <= degree) {
+                            const float bk = __ldg(&lb->hi[k]);
+                            sx = __fadd_rn(sx, __fmul_rn(c[k].x, bk));
+                            sy = __fadd_rn(sy, __fmul_rn(c[k].y, bk));
+                            sz = __fadd_rn(sz, __fmul_rn(c[k].z, bk));
+                        }
+                    }
+                    fx = __fsub_rn(sx, ox); fy = __fsub_rn(sy, oy); fz = __fsub_rn(sz, oz);
+                } else {
+                    fx = __fsub_rn(px, ox); fy = __fsub_rn(py, oy); fz = __fsub_rn(pz, oz);
+                }
+                float r = __fadd_rn(__fadd_rn(__fmul_rn(fx, rx), __fmul_rn(fy, ry)), __fmul_rn(fz, rz));
+                const float l = __fadd_rn(__fadd_rn(__fmul_rn(fx, lx), __fmul_rn(fy, ly)), __fmul_rn(fz, lz));
+                const float e = __fadd_rn(__fadd_rn(__fmul_rn(fx, ex), __fmul_rn(fy, ey)), __fmul_rn(fz, ez));
+                if (p.arc)
+                    r = copysignf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz))), r);
+                double t;
+                if (SPLINE) {
+                    // r*2.0/(c*dt) with dt = float(1/fs) (CpuAlgorithm.cpp:161-162)
+                    const float dt = (float)(1.0 / p.fs_d);
+                    t = __ddiv_rn(__dmul_rn((double)r, 2.0), (double)__fmul_rn(p.c, dt));
+                } else {
+                    t = __ddiv_rn(__dmul_rn(__dmul_rn((double)r, 2.0), p.fs_d), p.c_d);
+                }
+                const double fidx = floor(t + 0.5);
+                if (!(fidx >= 0.0 && fidx < (double)p.ns)) continue;
+                idx = (int)fidx;
+                if (BEAM == BEAM_GAUSSIAN) w = gauss_weight_ref(b, l, e);
+                else w = lut_weight_ref(b, r, l, e);
+                if (p.phase_delay) {
+                    const float ss_delay = (float)(((double)idx - t) / p.fs_d);
+                    const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
+                    sincosf(ph, &sph, &cph);
+                }
+            }
+            const float amp = w * a;
+            unsigned long long* dst = bins + ((int64_t)line * p.ns + idx) * stride;
+            if (p.phase_delay) {
+                bin_add(dst, amp * cph, p.scale);
+                bin_add(dst + 1, amp * sph, p.scale);
+            } else {
+                bin_add(dst, amp, p.scale);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+cudaError_t launch_prep_shared(const float4* xyza, int64_t n, int64_t off, const float origin[3], const SimParams& p,
+                               const BeamDev& b, uint32_t* keys, uint32_t* vals, float4* recA, float4* recB,
+                               cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t blocks = (n + threads - 1) / threads;
+    prep_shared_kernel<<<(unsigned)blocks, threads, 0, stream>>>(xyza, n, off, (double)origin[0], (double)origin[1],
+                                                                 (double)origin[2], origin[0], origin[1], origin[2],
+                                                                 p, b, keys, vals, recA, recB);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prep_shared_spline(const float4* cps, const float* amps, int64_t n, int num_cs, int first_cs,
+                                      int degree, const double* basis_d, const float* basis_f, int64_t off,
+                                      const float origin[3], const SimParams& p, const BeamDev& b, uint32_t* keys,
+                                      uint32_t* vals, float4* recA, float4* recB, cudaStream_t stream) {
+    (void)num_cs;
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    const int64_t blocks = (n + threads - 1) / threads;
+    prep_shared_spline_kernel<<<(unsigned)blocks, threads, 0, stream>>>(
+        cps, amps, n, first_cs, degree, basis_d, basis_f, off, (double)origin[0], (double)origin[1],
+        (double)origin[2], origin[0], origin[1], origin[2], p, b, keys, vals, recA, recB);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int* counts, cudaStream_t stream) {
+    init_counts_kernel<<<1, 1, 0, stream>>>(counts, n);
+    if (n > 0) {
+        const int threads = 256;
+        count_keys_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(sorted_keys, n, ns, counts);
+    }
+    finish_counts_kernel<<<1, 1, 0, stream>>>(counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts, int64_t n, const float4* recA,
+                                  const float4* recB, float4* out, int64_t plane, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int threads = 256;
+    gather_records_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(sorted_vals, counts, n,
+                                                                                        recA, recB, out, plane);
+    return cudaGetLastError();
+}
+
+template <bool PD, int BEAM, bool REF>
+static cudaError_t launch_shared_t(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
+                                   const LineGeom* lines, int L, const SimParams& p, const BeamDev& b,
+                                   unsigned long long* bins, cudaStream_t stream) {
+    const size_t smem = 2 * (size_t)chunk * sizeof(float4);
+    auto k = project_shared_kernel<PD, BEAM, REF>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
+    const int groups = (L + threads - 1) / threads;
+    const int64_t chunks = (n + chunk - 1) / chunk;
+    dim3 grid((unsigned)chunks, (unsigned)groups);
+    k<<<grid, threads, smem, stream>>>(records, plane, counts, chunk, lines, L, bins, p, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
+                                  const LineGeom* lines, int L, const SimParams& p, const BeamDev& b,
+                                  unsigned long long* bins, cudaStream_t stream) {
+    if (n <= 0 || L <= 0) return cudaSuccess;
+    const bool pd = p.phase_delay != 0;
+    const bool ref = p.mode == MODE_REFERENCE;
+#define BCSIM_SH(PDV, BM, R) launch_shared_t<PDV, BM, R>(records, plane, counts, n, chunk, lines, L, p, b, bins, stream)
+    if (b.type == BEAM_GAUSSIAN) {
+        if (pd) return ref ? BCSIM_SH(true, BEAM_GAUSSIAN, true) : BCSIM_SH(true, BEAM_GAUSSIAN, false);
+        return ref ? BCSIM_SH(false, BEAM_GAUSSIAN, true) : BCSIM_SH(false, BEAM_GAUSSIAN, false);
+    }
+    if (pd) return ref ? BCSIM_SH(true, BEAM_LUT, true) : BCSIM_SH(true, BEAM_LUT, false);
+    return ref ? BCSIM_SH(false, BEAM_LUT, true) : BCSIM_SH(false, BEAM_LUT, false);
+#undef BCSIM_SH
+}
+
+template <int BEAM, bool SPLINE, bool REF>
+static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const float* amps, int64_t n, int degree,
+                                    const uint32_t* index_list, const int* counts, int64_t list_lo,
+                                    const LineGeom* lines,
+                                    const int* line_ids, const LineTile* tiles, int num_tiles,
+                                    const LineBasis* basis, const SimParams& p, const BeamDev& b,
+                                    unsigned long long* bins, cudaStream_t stream) {
+    int64_t blocks = (n + GENERIC_THREADS - 1) / GENERIC_THREADS;
+    if (blocks > 1184) blocks = 1184;   // grid-stride beyond 8 waves of 152 SMs
+    if (index_list) blocks = 4;         // the near-origin residue is a handful of scatterers
+    if (blocks < 1) blocks = 1;
+    dim3 grid((unsigned)blocks, (unsigned)num_tiles);
+    project_generic_kernel<BEAM, SPLINE, REF><<<grid, GENERIC_THREADS, 0, stream>>>(
+        xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const float* amps, int64_t n, int num_cs,
+                                   int degree, const uint32_t* index_list, const int* counts, int64_t list_lo,
+                                   const LineGeom* lines, const int* line_ids, const LineTile* tiles, int num_tiles,
+                                   const LineBasis* basis, const SimParams& p, const BeamDev& b,
+                                   unsigned long long* bins, cudaStream_t stream) {
+    (void)num_cs;
+    if (n <= 0 || num_tiles <= 0) return cudaSuccess;
+    const bool spline = cps != nullptr;
+    const bool ref = p.mode == MODE_REFERENCE;
+#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream)
+    if (b.type == BEAM_GAUSSIAN) {
+        if (spline) return ref ? BCSIM_GEN(BEAM_GAUSSIAN, true, true) : BCSIM_GEN(BEAM_GAUSSIAN, true, false);
+        return ref ? BCSIM_GEN(BEAM_GAUSSIAN, false, true) : BCSIM_GEN(BEAM_GAUSSIAN, false, false);
+    }
+    if (spline) return ref ? BCSIM_GEN(BEAM_LUT, true, true) : BCSIM_GEN(BEAM_LUT, true, false);
+    return ref ? BCSIM_GEN(BEAM_LUT, false, true) : BCSIM_GEN(BEAM_LUT, false, false);
+#undef BCSIM_GEN
+}
+
+cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream) {
+    cudaError_t e = cudaMemcpyFromSymbolAsync(flag, g_bcsim_error_flag, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return e;
+    const int zero = 0;
+    return cudaMemcpyToSymbolAsync(g_bcsim_error_flag, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+}
+
+cudaError_t radix_sort_pairs(void* temp, size_t* temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,
+                             const uint32_t* vals_in, uint32_t* vals_out, int64_t n, int end_bit,
+                             cudaStream_t stream) {
+    return cub::DeviceRadixSort::SortPairs(temp, *temp_bytes, keys_in, keys_out, vals_in, vals_out, (int)n, 0,
+                                           end_bit, stream);
+}
+
+}  // namespace bcsim_gb300
