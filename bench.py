@@ -57,10 +57,44 @@ def flops_per_projection(lut: bool, phase_delay: bool) -> float:
     return f
 
 
-def make_job(name: str):
+def make_job(name: str, num_scatterers: int = 0, lines: str = ""):
+    """The named workload, optionally with fewer scatterers / lines (for
+    profiling captures on a small case)."""
     from openbcsim_gb300 import workloads as W
 
-    return getattr(W, name)()
+    kw = {}
+    if num_scatterers:
+        kw["num_scatterers"] = num_scatterers
+    if lines:
+        parts = [int(x) for x in lines.split(",")]
+        if name == "volume_3d_lut":
+            kw["n_az"], kw["n_el"] = parts[0], parts[-1]
+        else:
+            kw["num_lines"] = parts[0]
+    return getattr(W, name)(**kw)
+
+
+def run_simulate_only(args):
+    """Configure and run warmup + steps simulations, nothing else (the command
+    that profiling captures wrap)."""
+    import openbcsim_gb300 as gb
+
+    job = make_job(args.workload, args.num_scatterers, args.lines)
+    sim = gb.RfSimulator("gpu")
+    gb.configure_job(sim, job)
+    apply_params(sim, args.param)
+    out = None
+    for _ in range(args.warmup + args.steps):
+        out = sim.simulate_lines_line_major(out)
+    print(f"simulated {args.warmup + args.steps} x {job.name}: {job.num_scatterers} scatterers x "
+          f"{job.scan.num_lines} lines, |IQ|max {float(np.abs(out).max()):.4g}")
+
+
+def apply_params(sim, params):
+    """--param key=value pairs passed to set_parameter."""
+    for kv in params or []:
+        k, v = kv.split("=", 1)
+        sim.set_parameter(k, v)
 
 
 def rank_info():
@@ -135,10 +169,11 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     if world > 1 and not torch.distributed.is_initialized():
         torch.distributed.init_process_group("nccl")
-    job = make_job(args.workload)
+    job = make_job(args.workload, args.num_scatterers, args.lines)
     sim = gb.RfSimulator("gpu")
     sim.set_parameter("gpu_device", str(local))
     gb.configure_job(sim, job)
+    apply_params(sim, args.param)
     sim.set_parameter("store_kernel_details", "on")
     L, nd = sim.output_shape()
     dev_out = torch.empty((L, nd), dtype=torch.complex64, device="cuda")
@@ -361,9 +396,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-lines", type=int, default=64)
+    ap.add_argument("--num-scatterers", type=int, default=0, help="override the workload's scatterer count")
+    ap.add_argument("--lines", default="", help="override the line count (volume: 'n_az,n_el')")
+    ap.add_argument("--param", action="append", default=[], help="engine parameter key=value (repeatable)")
+    ap.add_argument("--simulate-only", action="store_true", help="only run warmup+steps simulations (profiling)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per projection launch from an ncu capture (reported as roofline.traffic)")
     args = ap.parse_args()
+    if args.simulate_only:
+        run_simulate_only(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     res = run_reference(args) if args.impl == "reference" else run_gpu(args)

@@ -164,6 +164,9 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
         if (!(v >= 0.0 && v < 1.0)) throw SimError(BCSIM_E_INVALID, "fir_tail_energy must be in [0, 1)");
         if (v != fir_tail_) tables_valid_ = false;
         fir_tail_ = v;
+    } else if (key == "cull") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        cull_ = b;
     } else if (key == "tile_lines") {
         const int v = std::stoi(value);
         if (v < 0) throw SimError(BCSIM_E_INVALID, "tile_lines must be >= 0");
@@ -197,6 +200,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "precision_mode") return mode_ == MODE_FP64 ? "fp64" : "reference";
     if (key == "fir_tail_energy") return fmt_double(fir_tail_);
     if (key == "tile_lines") return std::to_string(tile_lines_);
+    if (key == "cull") return cull_ ? "on" : "off";
     if (key == "fir_taps") return std::to_string(tap_count_);
     throw SimError(BCSIM_E_INVALID, "Illegal key: " + key);
 }
@@ -416,12 +420,92 @@ void Simulator::prepare_excitation_tables() {
                std::to_string(M_));
 }
 
+// Kernel line order for the shared-origin kernel: lines sorted along a Morton
+// curve over their directions (projected on the plane normal to the mean
+// direction), so that every 32 consecutive lines point in nearby directions,
+// and the bounding cone of each such slot of 32.
+static void order_lines(const std::vector<LineGeom>& lines, std::vector<int>& order, std::vector<SlotCone>& cones) {
+    const int L = (int)lines.size();
+    order.resize(L);
+    std::iota(order.begin(), order.end(), 0);
+    double m[3] = {0, 0, 0};
+    for (const auto& g : lines)
+        for (int k = 0; k < 3; k++) m[k] += g.d[k];
+    double mn = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    if (mn < 1e-12) { m[0] = 0; m[1] = 0; m[2] = 1; mn = 1; }
+    for (double& v : m) v /= mn;
+    // orthonormal e1, e2 perpendicular to m
+    double a[3] = {1, 0, 0};
+    if (std::fabs(m[0]) > 0.9) { a[0] = 0; a[1] = 1; }
+    double e1[3] = {a[1] * m[2] - a[2] * m[1], a[2] * m[0] - a[0] * m[2], a[0] * m[1] - a[1] * m[0]};
+    const double n1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (double& v : e1) v /= n1;
+    const double e2[3] = {m[1] * e1[2] - m[2] * e1[1], m[2] * e1[0] - m[0] * e1[2], m[0] * e1[1] - m[1] * e1[0]};
+    std::vector<double> u(L), v(L);
+    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
+    for (int i = 0; i < L; i++) {
+        const float* d = lines[i].d;
+        u[i] = d[0] * e1[0] + d[1] * e1[1] + d[2] * e1[2];
+        v[i] = d[0] * e2[0] + d[1] * e2[1] + d[2] * e2[2];
+        umin = std::min(umin, u[i]); umax = std::max(umax, u[i]);
+        vmin = std::min(vmin, v[i]); vmax = std::max(vmax, v[i]);
+    }
+    const double span = std::max(umax - umin, vmax - vmin) + 1e-12;
+    std::vector<uint32_t> key(L);
+    for (int i = 0; i < L; i++) {
+        const uint32_t qu = (uint32_t)std::min(65535.0, (u[i] - umin) / span * 65535.0);
+        const uint32_t qv = (uint32_t)std::min(65535.0, (v[i] - vmin) / span * 65535.0);
+        uint32_t k = 0;
+        for (int bit = 0; bit < 16; bit++) k |= ((qu >> bit) & 1u) << (2 * bit) | ((qv >> bit) & 1u) << (2 * bit + 1);
+        key[i] = k;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+    const int slots = (L + 31) / 32;
+    cones.assign(slots, SlotCone{0, 0, 1, -1, 0, 0, 0, 0});
+    for (int s = 0; s < slots; s++) {
+        double c[3] = {0, 0, 0};
+        const int lo = s * 32, hi = std::min(L, lo + 32);
+        for (int i = lo; i < hi; i++)
+            for (int k = 0; k < 3; k++) c[k] += lines[order[i]].d[k];
+        const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        double alpha = M_PI;
+        if (cn > 1e-9) {
+            for (double& x : c) x /= cn;
+            alpha = 0.0;
+            for (int i = lo; i < hi; i++) {
+                const float* d = lines[order[i]].d;
+                const double dn = std::sqrt((double)d[0] * d[0] + (double)d[1] * d[1] + (double)d[2] * d[2]);
+                const double cosang = std::max(-1.0, std::min(1.0, (d[0] * c[0] + d[1] * c[1] + d[2] * c[2]) / dn));
+                alpha = std::max(alpha, std::acos(cosang));
+            }
+            alpha += 1e-4;   // margin for float rounding of the axis and the test
+        }
+        SlotCone cone;
+        cone.cx = (float)c[0]; cone.cy = (float)c[1]; cone.cz = (float)c[2];
+        cone.cos_a = alpha >= M_PI / 2 ? -1.0f : (float)std::cos(alpha);
+        cone.sin_a = alpha >= M_PI / 2 ? 1.0f : (float)std::sin(alpha);
+        cone.pad0 = cone.pad1 = cone.pad2 = 0.0f;
+        cones[s] = cone;
+    }
+}
+
 void Simulator::prepare_lines() {
     if (lines_valid_) return;
     lines_dev_.reserve(std::max<size_t>(1, lines_.size()) * sizeof(LineGeom));
     if (!lines_.empty())
         BCSIM_CUDA(cudaMemcpyAsync(lines_dev_.get(), lines_.data(), lines_.size() * sizeof(LineGeom),
                                    cudaMemcpyHostToDevice, stream_));
+    std::vector<int> order;
+    std::vector<SlotCone> cones;
+    order_lines(lines_, order, cones);
+    line_order_dev_.reserve(std::max<size_t>(1, order.size()) * sizeof(int));
+    cones_dev_.reserve(std::max<size_t>(1, cones.size()) * sizeof(SlotCone));
+    if (!order.empty()) {
+        BCSIM_CUDA(cudaMemcpyAsync(line_order_dev_.get(), order.data(), order.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice, stream_));
+        BCSIM_CUDA(cudaMemcpyAsync(cones_dev_.get(), cones.data(), cones.size() * sizeof(SlotCone),
+                                   cudaMemcpyHostToDevice, stream_));
+    }
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
     lines_valid_ = true;
 }
@@ -550,6 +634,23 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     S = std::max(-100, std::min(100, S));
     p.log2scale = S;
     p.scale = std::ldexp(1.0f, S);
+    // exact culling radius (fp64 mode): beyond it the weight is exactly 0
+    if (mode_ == MODE_FP64 && cull_) {
+        double r = 0.0;
+        if (beam_type_ == BEAM_GAUSSIAN) {
+            // exp2f(-q) is exactly 0 for q >= 151, q = l^2 gl + e^2 ge >= dist^2 min(gl, ge)
+            r = std::sqrt(151.0 / std::min((double)b.gl, (double)b.ge));
+        } else {
+            // table coordinate -1 < t < n-1  <=>  first - spacing < x < last
+            const double rl = std::max(std::fabs((double)lut_ext_[2] - b.dl), std::fabs((double)lut_ext_[3]));
+            const double re = std::max(std::fabs((double)lut_ext_[4] - b.de), std::fabs((double)lut_ext_[5]));
+            r = std::sqrt(rl * rl + re * re);
+        }
+        r = r * 1.001 + 1e-7;
+        p.cull = std::isfinite(r) ? 1 : 0;
+        p.cull_r = (float)r;
+        p.cull_r2 = (float)(r * r);
+    }
 
     const int stride = phase_delay_ ? 2 : 1;
     const size_t bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
@@ -738,12 +839,11 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
         if (store_details_) debug_["prep_sort_ms"].push_back(timer.stop());
         timer.restart();
         // records per CTA: enough CTAs to fill the GPU several times over
-        const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
-        const int64_t groups = (L + threads - 1) / threads;
-        int chunk = 2048;
-        while (chunk > 256 && ((N + chunk - 1) / chunk) * groups < 8 * 152) chunk /= 2;
+        int chunk = 1024;
+        while (chunk > 128 && (N + chunk - 1) / chunk < 4 * 152) chunk /= 2;
         if (tile_lines_ > 0) chunk = std::max(64, std::min(4096, tile_lines_));
-        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, chunk, lines_d, L, p, b, bins, st));
+        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, chunk, lines_d,
+                                         line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins, st));
         // near-origin residue, per pair
         for (const GenLaunch& g : gl) {
             if (g.kind == 0) {

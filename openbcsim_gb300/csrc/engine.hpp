@@ -114,6 +114,7 @@ private:
     int mode_ = MODE_FP64;
     double fir_tail_ = 1e-10;
     int tile_lines_ = 0;   // 0 = automatic
+    bool cull_ = true;     // exact culling of zero-weight (scatterer, line-slot) pairs
 
     bool excitation_set_ = false;
     std::vector<float> taps_;
@@ -152,7 +153,7 @@ private:
     int64_t tap_start_ = 0, tap_count_ = 0;
     DeviceBuffer taps_dev_, demod_dev_;
     bool lines_valid_ = false;
-    DeviceBuffer lines_dev_;
+    DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;
     DeviceBuffer bins_, out_;
     DeviceBuffer keys_in_, vals_in_, keys_out_, vals_out_, recA_, recB_, records_, sort_tmp_, counts_;
     DeviceBuffer gen_tiles_, gen_line_ids_, gen_basis_, spl_basis_d_, spl_basis_f_;

@@ -47,6 +47,16 @@ struct SimParams {
     float two_pi_fd_over_fs;   // phase per sample of sub-sample delay
     float scale;               // fixed-point scale 2^S for bin accumulation
     int log2scale;
+    // exact culling in the shared-origin kernel: a scatterer farther than
+    // cull_radius from a line's axis has weight exactly 0 on that line
+    int cull;
+    float cull_r2, cull_r;
+};
+
+// Bounding cone of a slot of 32 lines (consecutive in the kernel's line order):
+// every line direction is within angle alpha of the unit axis c.
+struct SlotCone {
+    float cx, cy, cz, cos_a, sin_a, pad0, pad1, pad2;
 };
 
 // A tile of lines for the per-pair projection kernel: `count` lines taken from
@@ -99,10 +109,12 @@ cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts
                                   const float4* recB, float4* out, int64_t plane, cudaStream_t stream);
 
 // Projection of the counts[0] sorted records onto all lines (lines share the
-// origin); `chunk` records per CTA, one line per thread.
+// origin); `chunk` records per CTA, lines taken in the order line_order[] with
+// slot cones[] per 32 of them.
 cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
-                                  const LineGeom* lines, int num_lines, const SimParams& p, const BeamDev& b,
-                                  unsigned long long* bins, cudaStream_t stream);
+                                  const LineGeom* lines, const int* line_order, const SlotCone* cones,
+                                  int num_lines, const SimParams& p, const BeamDev& b, unsigned long long* bins,
+                                  cudaStream_t stream);
 
 // Per-pair projection: fixed scatterers (cps == nullptr) or splines, arbitrary
 // lines.  If index_list is given, the entries index_list[counts[0] ...

@@ -322,18 +322,52 @@ __device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
 // Records per folding of the FP32 run sum into the integer bin total: bounds
 // the length of any FP32 summation to FOLD terms.
 constexpr int FOLD = 128;
+// Lines per thread in the shared-origin kernel.
+constexpr int LPT = 2;
 
-// One CTA: a chunk of `chunk` consecutive records (sorted by bin) x one line
-// per thread.  Every thread walks the same records in the same order (records
-// are broadcast from shared memory, the bin-change branch is warp-uniform),
-// sums its line's contributions of a bin in FP32, folds into an int64 total
-// every FOLD records and writes the bin when the bin changes: with a plain
-// store for bins that lie strictly inside the chunk (no other CTA has records
-// there), with an integer atomic for the chunk's first and last bin.
+// Per-line constants of the shared-origin kernel (fp64 mode):
+//   Gaussian: u = lateral * sqrt(gl), v = elevational * sqrt(ge), so that the
+//             weight is exp2(-((d.u)^2 + (d.v)^2));
+//   LUT:      u = lateral / dl, v = elevational / de, ou = -l_first / dl,
+//             ov = -e_first / de: table coordinates tl = d.u + ou, te = d.v + ov.
+struct LineK {
+    float rx, ry, rz, ux, uy, uz, vx, vy, vz, ou, ov;
+};
+
+template <int BEAM, bool REF>
+__device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) {
+    LineK k;
+    k.rx = __ldg(&g->d[0]); k.ry = __ldg(&g->d[1]); k.rz = __ldg(&g->d[2]);
+    const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
+    const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
+    float su = 1.0f, sv = 1.0f;
+    k.ou = 0.0f; k.ov = 0.0f;
+    if (!REF) {
+        if (BEAM == BEAM_GAUSSIAN) {
+            su = sqrtf(b.gl); sv = sqrtf(b.ge);
+        } else {
+            su = b.inv_dl; sv = b.inv_de;
+            k.ou = -b.lf * b.inv_dl; k.ov = -b.ef * b.inv_de;
+        }
+    }
+    k.ux = lx * su; k.uy = ly * su; k.uz = lz * su;
+    k.vx = ex * sv; k.vy = ey * sv; k.vz = ez * sv;
+    return k;
+}
+
+// One CTA: a chunk of `chunk` consecutive records (sorted by bin) staged once in
+// shared memory by a TMA bulk copy, then for every group of blockDim * LPT
+// lines, each thread walks all records for its LPT lines.  Records are
+// broadcast from shared memory and the bin-change branch is warp-uniform; a
+// line's contributions to one bin are summed in FP32, folded into an int64
+// total every FOLD records, and written when the bin changes -- a plain store
+// for bins strictly inside the chunk (no other CTA holds records there), an
+// integer atomic for the chunk's first and last bin.
 template <bool PD, int BEAM, bool REF>
 __global__ void __launch_bounds__(256)
     project_shared_kernel(const float4* __restrict__ records, int64_t plane, const int* __restrict__ counts, int chunk,
-                          const LineGeom* __restrict__ lines, int L, unsigned long long* __restrict__ bins,
+                          const LineGeom* __restrict__ lines, const int* __restrict__ line_order,
+                          const SlotCone* __restrict__ cones, int L, unsigned long long* __restrict__ bins,
                           SimParams p, BeamDev b) {
     extern __shared__ __align__(128) float4 sm[];
     __shared__ __align__(8) uint64_t bar;
@@ -356,12 +390,6 @@ __global__ void __launch_bounds__(256)
         bulk_load(smA, records + start, bytes, &bar);
         bulk_load(smB, records + plane + start, bytes, &bar);
     }
-    const int line = blockIdx.y * blockDim.x + tid;
-    const bool active = line < L;
-    const LineGeom* g = lines + (active ? line : L - 1);
-    const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
-    const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
-    const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
     if (!mbar_wait(&bar, 0, 1u << 26)) {
         g_bcsim_error_flag = 1;
         mbar_wait(&bar, 0, 1u << 26);
@@ -369,85 +397,146 @@ __global__ void __launch_bounds__(256)
     }
 
     const int stride = PD ? 2 : 1;
-    unsigned long long* lbins = bins + (int64_t)(active ? line : 0) * p.ns * stride;
     const float scale = p.scale;
     const int first_bin = __float_as_int(smB[0].w);
     const int last_bin = __float_as_int(smB[cnt - 1].w);
-    int cur = first_bin;
-    long long tot_r = 0, tot_i = 0;
-    float ar = 0.0f, ai = 0.0f;
-    int since_fold = 0;
+    // lookup-table coordinate ranges -1 < t < n-1 as |t - c| < h
+    const float cl = 0.5f * (float)(b.nl - 2), hl = 0.5f * (float)b.nl;
+    const float ce = 0.5f * (float)(b.ne - 2), he = 0.5f * (float)b.ne;
 
-    for (int i = 0; i < cnt; i++) {
-        const float4 B = smB[i];
-        const int idx = __float_as_int(B.w);
-        if (idx != cur) {
-            tot_r += __float2ll_rn(ar * scale);
-            if (PD) tot_i += __float2ll_rn(ai * scale);
-            if (active) {
-                if (cur == first_bin || cur == last_bin) {
-                    if (tot_r) atomicAdd(lbins + (int64_t)cur * stride, (unsigned long long)tot_r);
-                    if (PD && tot_i) atomicAdd(lbins + (int64_t)cur * stride + 1, (unsigned long long)tot_i);
-                } else {
-                    if (tot_r) lbins[(int64_t)cur * stride] = (unsigned long long)tot_r;
-                    if (PD && tot_i) lbins[(int64_t)cur * stride + 1] = (unsigned long long)tot_i;
+    const bool cull = !REF && p.cull;
+    for (int g0 = 0; g0 < L; g0 += blockDim.x * LPT) {
+        LineK k[LPT];
+        bool active[LPT];
+        unsigned long long* lb[LPT];
+        float ccx[LPT], ccy[LPT], ccz[LPT], cca[LPT], csa[LPT];
+#pragma unroll
+        for (int j = 0; j < LPT; j++) {
+            const int slot_pos = g0 + j * blockDim.x + tid;
+            active[j] = slot_pos < L;
+            const int line = __ldg(line_order + (active[j] ? slot_pos : L - 1));
+            k[j] = load_line<BEAM, REF>(lines + line, b);
+            lb[j] = bins + (int64_t)line * p.ns * stride;
+            // cone of this warp's 32 lines (slot_pos / 32 is uniform in the warp)
+            const SlotCone* c = cones + min(slot_pos, L - 1) / 32;
+            ccx[j] = __ldg(&c->cx); ccy[j] = __ldg(&c->cy); ccz[j] = __ldg(&c->cz);
+            cca[j] = __ldg(&c->cos_a); csa[j] = __ldg(&c->sin_a) * p.cull_r;
+        }
+        int cur = first_bin;
+        long long tr[LPT], ti[LPT];
+        float ar[LPT], ai[LPT];
+#pragma unroll
+        for (int j = 0; j < LPT; j++) { tr[j] = 0; ti[j] = 0; ar[j] = 0.0f; ai[j] = 0.0f; }
+
+        for (int i = 0; i < cnt; i++) {
+            const float4 B = smB[i];
+            const int idx = __float_as_int(B.w);
+            if (idx != cur || (i & (FOLD - 1)) == FOLD - 1) {
+#pragma unroll
+                for (int j = 0; j < LPT; j++) {
+                    tr[j] += __float2ll_rn(ar[j] * scale);
+                    if (PD) ti[j] += __float2ll_rn(ai[j] * scale);
+                    ar[j] = 0.0f;
+                    ai[j] = 0.0f;
+                }
+                if (idx != cur) {
+                    const bool edge = cur == first_bin || cur == last_bin;
+#pragma unroll
+                    for (int j = 0; j < LPT; j++) {
+                        if (active[j]) {
+                            unsigned long long* dst = lb[j] + (int64_t)cur * stride;
+                            if (edge) {
+                                if (tr[j]) atomicAdd(dst, (unsigned long long)tr[j]);
+                                if (PD && ti[j]) atomicAdd(dst + 1, (unsigned long long)ti[j]);
+                            } else {
+                                if (tr[j]) dst[0] = (unsigned long long)tr[j];
+                                if (PD && ti[j]) dst[1] = (unsigned long long)ti[j];
+                            }
+                        }
+                        tr[j] = 0;
+                        ti[j] = 0;
+                    }
+                    cur = idx;
                 }
             }
-            cur = idx;
-            tot_r = tot_i = 0;
-            ar = ai = 0.0f;
-            since_fold = 0;
-        } else if (since_fold == FOLD) {
-            tot_r += __float2ll_rn(ar * scale);
-            if (PD) tot_i += __float2ll_rn(ai * scale);
-            ar = ai = 0.0f;
-            since_fold = 0;
-        }
-        since_fold++;
-        const float4 A = smA[i];
-        float l, e, dot;
-        if (REF) {
-            // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
-            dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, rx), __fmul_rn(A.y, ry)), __fmul_rn(A.z, rz));
-            l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, lx), __fmul_rn(A.y, ly)), __fmul_rn(A.z, lz));
-            e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, ex), __fmul_rn(A.y, ey)), __fmul_rn(A.z, ez));
-        } else {
-            dot = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
-            l = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
-            e = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
-        }
-        float w;
-        if (BEAM == BEAM_GAUSSIAN) {
-            if (REF) w = gauss_weight_ref(b, l, e);
-            else w = exp2f(-fmaf(l * l, b.gl, e * e * b.ge));
-        } else {
-            if (REF) {
-                // the reference recomputes the radial table coordinate per pair from r
-                w = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
-                                                          __fmul_rn(A.z, A.z))),
-                                   l, e);
-            } else {
-                const float tl = (l - b.lf) * b.inv_dl;
-                const float te = (e - b.ef) * b.inv_de;
-                w = lut_weight_packed(b, __float_as_int(B.z), B.y, tl, te);
+            const float4 A = smA[i];
+            // the scatterer sits farther than cull_r from every axis of a slot when
+            // its angle to the slot axis exceeds alpha + asin(cull_r / rho):
+            // cos(angle) < (sqrt(rho^2 - r^2) cos(alpha) - r sin(alpha)) / rho
+            float sfar = 0.0f;
+            if (cull) sfar = sqrtf(fmaxf(fmaf(A.z, A.z, fmaf(A.y, A.y, A.x * A.x)) - p.cull_r2, 0.0f));
+#pragma unroll
+            for (int j = 0; j < LPT; j++) {
+                const LineK& q = k[j];
+                if (cull) {
+                    const float dc = fmaf(A.z, ccz[j], fmaf(A.y, ccy[j], A.x * ccx[j]));
+                    if (dc < fmaf(sfar, cca[j], -csa[j])) continue;   // warp-uniform
+                }
+                float w;
+                if (REF) {
+                    // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
+                    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
+                    const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
+                    const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
+                    if (BEAM == BEAM_GAUSSIAN) {
+                        w = gauss_weight_ref(b, l, e);
+                    } else {
+                        // the reference recomputes the radial table coordinate per pair from r
+                        w = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                                  __fmul_rn(A.z, A.z))),
+                                           l, e);
+                    }
+                    w = signbit(dot) ? 0.0f : w;
+                } else {
+                    const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
+                    const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
+                    const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
+                    if (BEAM == BEAM_GAUSSIAN) {
+                        w = exp2f(-fmaf(u, u, v * v));
+                        // arc projection: a line for which the scatterer lies behind the
+                        // origin sees it at -rho, outside [0, ns) for every record
+                        // (near-origin scatterers take the per-pair path)
+                        w = signbit(dot) ? 0.0f : w;
+                    } else {
+                        w = 0.0f;
+                        if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
+                            const int l0 = (int)u, e0 = (int)v;
+                            const float fl = u < 0.0f ? 0.0f : u - (float)l0;
+                            const float fe = v < 0.0f ? 0.0f : v - (float)e0;
+                            const int base = (__float_as_int(B.z) * b.nl + l0) * b.ne + e0;
+                            const float4 P = __ldg(b.lut4 + base);
+                            const float4 Q = __ldg(b.lut4 + base + b.ne);
+                            const float fr = B.y;
+                            // radial, lateral, elevational (BeamProfile.cpp:116-127)
+                            const float c00 = fmaf(fr, P.z - P.x, P.x);
+                            const float c01 = fmaf(fr, P.w - P.y, P.y);
+                            const float c10 = fmaf(fr, Q.z - Q.x, Q.x);
+                            const float c11 = fmaf(fr, Q.w - Q.y, Q.y);
+                            const float c0 = fmaf(fl, c10 - c00, c00);
+                            const float c1 = fmaf(fl, c11 - c01, c01);
+                            w = fmaf(fe, c1 - c0, c0);
+                        }
+                    }
+                }
+                ar[j] = fmaf(w, A.w, ar[j]);
+                if (PD) ai[j] = fmaf(w, B.x, ai[j]);
             }
         }
-        // arc projection: a line for which the scatterer lies behind the origin
-        // sees it at -rho, outside [0, ns) for every record (near-origin
-        // scatterers take the per-pair path)
-        w = signbit(dot) ? 0.0f : w;
-        ar = fmaf(w, A.w, ar);
-        if (PD) ai = fmaf(w, B.x, ai);
-    }
-    tot_r += __float2ll_rn(ar * scale);
-    if (PD) tot_i += __float2ll_rn(ai * scale);
-    if (active) {
-        if (cur == first_bin || cur == last_bin) {
-            if (tot_r) atomicAdd(lbins + (int64_t)cur * stride, (unsigned long long)tot_r);
-            if (PD && tot_i) atomicAdd(lbins + (int64_t)cur * stride + 1, (unsigned long long)tot_i);
-        } else {
-            if (tot_r) lbins[(int64_t)cur * stride] = (unsigned long long)tot_r;
-            if (PD && tot_i) lbins[(int64_t)cur * stride + 1] = (unsigned long long)tot_i;
+        const bool edge = cur == first_bin || cur == last_bin;
+#pragma unroll
+        for (int j = 0; j < LPT; j++) {
+            tr[j] += __float2ll_rn(ar[j] * scale);
+            if (PD) ti[j] += __float2ll_rn(ai[j] * scale);
+            if (active[j]) {
+                unsigned long long* dst = lb[j] + (int64_t)cur * stride;
+                if (edge) {
+                    if (tr[j]) atomicAdd(dst, (unsigned long long)tr[j]);
+                    if (PD && ti[j]) atomicAdd(dst + 1, (unsigned long long)ti[j]);
+                } else {
+                    if (tr[j]) dst[0] = (unsigned long long)tr[j];
+                    if (PD && ti[j]) dst[1] = (unsigned long long)ti[j];
+                }
+            }
         }
     }
 }
@@ -667,27 +756,30 @@ cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts
 
 template <bool PD, int BEAM, bool REF>
 static cudaError_t launch_shared_t(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
-                                   const LineGeom* lines, int L, const SimParams& p, const BeamDev& b,
-                                   unsigned long long* bins, cudaStream_t stream) {
+                                   const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
+                                   const SimParams& p, const BeamDev& b, unsigned long long* bins,
+                                   cudaStream_t stream) {
     const size_t smem = 2 * (size_t)chunk * sizeof(float4);
     auto k = project_shared_kernel<PD, BEAM, REF>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
-    const int groups = (L + threads - 1) / threads;
+    const int per = (L + LPT - 1) / LPT;
+    const int threads = per >= 256 ? 256 : ((per + 31) / 32) * 32;
     const int64_t chunks = (n + chunk - 1) / chunk;
-    dim3 grid((unsigned)chunks, (unsigned)groups);
-    k<<<grid, threads, smem, stream>>>(records, plane, counts, chunk, lines, L, bins, p, b);
+    k<<<(unsigned)chunks, threads, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
+                                                   p, b);
     return cudaGetLastError();
 }
 
 cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
-                                  const LineGeom* lines, int L, const SimParams& p, const BeamDev& b,
-                                  unsigned long long* bins, cudaStream_t stream) {
+                                  const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
+                                  const SimParams& p, const BeamDev& b, unsigned long long* bins,
+                                  cudaStream_t stream) {
     if (n <= 0 || L <= 0) return cudaSuccess;
     const bool pd = p.phase_delay != 0;
     const bool ref = p.mode == MODE_REFERENCE;
-#define BCSIM_SH(PDV, BM, R) launch_shared_t<PDV, BM, R>(records, plane, counts, n, chunk, lines, L, p, b, bins, stream)
+#define BCSIM_SH(PDV, BM, R) \
+    launch_shared_t<PDV, BM, R>(records, plane, counts, n, chunk, lines, line_order, cones, L, p, b, bins, stream)
     if (b.type == BEAM_GAUSSIAN) {
         if (pd) return ref ? BCSIM_SH(true, BEAM_GAUSSIAN, true) : BCSIM_SH(true, BEAM_GAUSSIAN, false);
         return ref ? BCSIM_SH(false, BEAM_GAUSSIAN, true) : BCSIM_SH(false, BEAM_GAUSSIAN, false);

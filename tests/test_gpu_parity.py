@@ -163,3 +163,20 @@ def test_full_size_lines_vs_oracle(oracle, which):
     for lo in (0, L // 2 - 2, L - 4):
         ref = oracle.simulate(job, oracle.MODE_FP64, line_begin=lo, line_end=lo + 4)
         assert oracle.rel_rms(iq[lo:lo + 4], ref) <= FP64_TOL, (which, lo)
+
+
+@pytest.mark.parametrize("name", ["sector_pd", "sector_nopd", "lut3d", "edge"])
+def test_culling_is_exact(name):
+    """Skipping (scatterer, line-slot) pairs whose weight is provably zero
+    changes no bit of the output."""
+    job, _ = load_golden(name)
+    a = run(job, cull="on")
+    b = run(job, cull="off")
+    assert np.array_equal(a, b)
+
+
+def test_culling_is_exact_full_volume():
+    from openbcsim_gb300 import workloads as W
+
+    job = W.volume_3d_lut(num_scatterers=300_000, n_az=48, n_el=40)
+    assert np.array_equal(run(job, cull="on"), run(job, cull="off"))
