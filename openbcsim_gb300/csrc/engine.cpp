@@ -498,6 +498,8 @@ void Simulator::prepare_lines() {
     std::vector<int> order;
     std::vector<SlotCone> cones;
     order_lines(lines_, order, cones);
+    line_rank_.assign(order.size(), 0);
+    for (size_t i = 0; i < order.size(); i++) line_rank_[order[i]] = (int)i;
     line_order_dev_.reserve(std::max<size_t>(1, order.size()) * sizeof(int));
     cones_dev_.reserve(std::max<size_t>(1, cones.size()) * sizeof(SlotCone));
     if (!order.empty()) {
@@ -713,11 +715,15 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     }
 
     // line tiles for the per-pair kernel
+    // lines of a tile: same knot interval (splines), nearby directions
     auto make_tiles = [&](const std::vector<int>* mu, std::vector<int>& ids, std::vector<LineTile>& tiles) {
         ids.resize(L);
         std::iota(ids.begin(), ids.end(), 0);
-        if (mu) std::stable_sort(ids.begin(), ids.end(), [&](int a, int c) { return (*mu)[a] < (*mu)[c]; });
-        const int per = tile_lines_ > 0 ? tile_lines_ : 8;
+        std::sort(ids.begin(), ids.end(), [&](int a, int c) {
+            const int ma = mu ? (*mu)[a] : 0, mc = mu ? (*mu)[c] : 0;
+            return ma != mc ? ma < mc : line_rank_[a] < line_rank_[c];
+        });
+        const int per = tile_lines_ > 0 ? std::min(tile_lines_, PAIR_THREADS) : PAIR_THREADS;
         tiles.clear();
         int i = 0;
         while (i < L) {

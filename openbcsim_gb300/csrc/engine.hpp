@@ -154,6 +154,7 @@ private:
     DeviceBuffer taps_dev_, demod_dev_;
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;
+    std::vector<int> line_rank_;   // position of each line in the direction-ordered sequence
     DeviceBuffer bins_, out_;
     DeviceBuffer keys_in_, vals_in_, keys_out_, vals_out_, recA_, recB_, records_, sort_tmp_, counts_;
     DeviceBuffer gen_tiles_, gen_line_ids_, gen_basis_, spl_basis_d_, spl_basis_f_;

@@ -68,6 +68,9 @@ struct LineTile {
     int pad;
 };
 
+// Lines per CTA of the per-pair kernel (the largest line tile).
+constexpr int PAIR_THREADS = 128;
+
 // Per-line spline basis: p+1 non-zero basis values as float pairs (hi, lo),
 // starting at control point mu - degree.
 constexpr int MAX_SPLINE_DEGREE = 7;

@@ -544,165 +544,260 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 // per-pair projection
 // ---------------------------------------------------------------------------
-constexpr int GENERIC_THREADS = 256;
+// Scatterers per staged chunk of the per-pair kernel (lines per CTA:
+// PAIR_THREADS in kernels.hpp).
+constexpr int PAIR_CHUNK = 256;
 
+// Exact arc-projection time of flight of one pair in float-pair arithmetic (fp64 mode).
+// (dx, dy, dz): the scatterer relative to the line origin as pairs.  Returns
+// false if the bin is outside [0, ns); otherwise the bin and the sub-sample
+// delay idx - t in samples.
+__device__ __forceinline__ bool pair_bin(df dx, df dy, df dz, float dot, const SimParams& p, int* idx_out,
+                                         float* delay_out, float* r_out) {
+    df r;
+    {
+        // arc projection: r = +-|d|, |d|^2 = sum hi^2 (exact products) + 2 hi lo
+        const df x2 = two_prod(dx.hi, dx.hi), y2 = two_prod(dy.hi, dy.hi), z2 = two_prod(dz.hi, dz.hi);
+        df s = two_sum(x2.hi, y2.hi);
+        const df s2 = two_sum(s.hi, z2.hi);
+        float lo = s.lo + s2.lo + x2.lo + y2.lo + z2.lo;
+        lo = fmaf(2.0f * dx.hi, dx.lo, lo);
+        lo = fmaf(2.0f * dy.hi, dy.lo, lo);
+        lo = fmaf(2.0f * dz.hi, dz.lo, lo);
+        r = df_sqrt(fast_two_sum(s2.hi, lo));
+        if (signbit(dot)) { r.hi = -r.hi; r.lo = -r.lo; }
+    }
+    *r_out = r.hi + r.lo;
+    const df t = df_mul(r, df_make(p.k_hi, p.k_lo));
+    // idx = floor(t + 0.5) decided on the pair: with f = floor(hi) the remainder
+    // hi - f is exact, so compare (hi - f - 0.5) with -lo.
+    float f = floorf(t.hi);
+    float rem = t.hi - f;
+    if (rem + t.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
+    const bool up = (rem - 0.5f) >= -t.lo;
+    const float fidx = up ? f + 1.0f : f;
+    if (!(fidx >= 0.0f && fidx < (float)p.ns)) return false;
+    *idx_out = (int)fidx;
+    *delay_out = (up ? 1.0f : 0.0f) - rem - t.lo;
+    return true;
+}
+
+// Per (scatterer, line) pair projection for any line geometry and for splines.
+// CTA = a tile of up to PAIR_THREADS lines (one per thread; for splines all with
+// the same knot interval mu) x a chunk of PAIR_CHUNK scatterers staged in shared
+// memory and broadcast to the threads.  Each pair first gets an FP32 position
+// and weight; a pair whose contribution rounds to zero in the fixed-point bins
+// (or lies outside the lookup table by a margin) is skipped -- exactly, since it
+// would add 0 -- and only the remaining pairs compute the float-pair time of
+// flight and add their contribution with integer atomics.
 template <int BEAM, bool SPLINE, bool REF>
-__global__ void __launch_bounds__(GENERIC_THREADS)
+__global__ void __launch_bounds__(PAIR_THREADS)
     project_generic_kernel(const float4* __restrict__ xyza, const float4* __restrict__ cps,
                            const float* __restrict__ amps, int64_t n, int degree,
                            const uint32_t* __restrict__ index_list, const int* __restrict__ counts,
                            int64_t list_lo, const LineGeom* __restrict__ lines, const int* __restrict__ line_ids,
                            const LineTile* __restrict__ tiles, const LineBasis* __restrict__ basis,
                            unsigned long long* __restrict__ bins, SimParams p, BeamDev b) {
+    __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? MAX_SPLINE_DEGREE + 1 : 1)];
+    __shared__ float sa[PAIR_CHUNK];
     const LineTile tile = tiles[blockIdx.y];
-    int64_t count = n;
-    int64_t list_off = 0;
+    int64_t count = n, list_off = 0;
     if (index_list) {
         list_off = __ldg(counts);
         count = __ldg(counts + 1);
     }
+    const int tid = threadIdx.x;
+    const int np = degree + 1;
+    const bool active = tid < tile.count;
+    const int line = __ldg(line_ids + tile.first + (active ? tid : 0));
+    const LineGeom* g = lines + line;
+    const float ox = __ldg(&g->o[0]), oy = __ldg(&g->o[1]), oz = __ldg(&g->o[2]);
+    const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
+    const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
+    const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
+    float bh[MAX_SPLINE_DEGREE + 1], bl[MAX_SPLINE_DEGREE + 1];
+    if (SPLINE) {
+        const LineBasis* lb = basis + line;
+#pragma unroll
+        for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+            bh[k] = k < np ? __ldg(&lb->hi[k]) : 0.0f;
+            bl[k] = k < np ? __ldg(&lb->lo[k]) : 0.0f;
+        }
+    }
     const int stride = p.phase_delay ? 2 : 1;
-    for (int64_t s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s0 < count;
-         s0 += (int64_t)gridDim.x * blockDim.x) {
-        int64_t s = s0;
+    unsigned long long* lbins = bins + (int64_t)line * p.ns * stride;
+    // a contribution below half a fixed-point unit rounds to 0
+    const float skip_below = 0.499f / p.scale;
+    const float gl = b.gl, ge = b.ge;
+
+    for (int64_t c0 = (int64_t)blockIdx.x * PAIR_CHUNK; c0 < count; c0 += (int64_t)gridDim.x * PAIR_CHUNK) {
+    const int cnt = (int)min((int64_t)PAIR_CHUNK, count - c0);
+    __syncthreads();   // the previous chunk is consumed
+    // stage the chunk (gathering through the index list for the near-origin residue)
+    for (int i = tid; i < cnt; i += blockDim.x) {
+        int64_t s = c0 + i;
+        bool ok = true;
         if (index_list) {
-            s = (int64_t)__ldg(index_list + list_off + s0) - list_lo;
-            if (s < 0 || s >= n) continue;
+            s = (int64_t)__ldg(index_list + list_off + s) - list_lo;
+            ok = s >= 0 && s < n;
         }
-        float a;
-        float4 c[MAX_SPLINE_DEGREE + 1];
-        float px = 0.f, py = 0.f, pz = 0.f;
         if (SPLINE) {
-            a = __ldg(amps + s);
-#pragma unroll
-            for (int k = 0; k <= MAX_SPLINE_DEGREE; k++)
-                if (k <= degree) c[k] = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+            for (int k = 0; k < np; k++)
+                sp[i * np + k] = ok ? __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+            sa[i] = ok ? __ldg(amps + s) : 0.0f;
         } else {
-            const float4 q = __ldg(xyza + s);
-            px = q.x; py = q.y; pz = q.z; a = q.w;
+            const float4 q = ok ? __ldg(xyza + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+            sp[i] = q;
+            sa[i] = ok ? q.w : 0.0f;
         }
-        for (int j = 0; j < tile.count; j++) {
-            const int line = __ldg(line_ids + tile.first + j);
-            const LineGeom* g = lines + line;
-            const float ox = __ldg(&g->o[0]), oy = __ldg(&g->o[1]), oz = __ldg(&g->o[2]);
-            const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
-            const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
-            const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
-            float w, cph = 1.0f, sph = 0.0f;
-            int idx;
-            if (!REF) {
-                // position relative to the origin as float pairs
-                df dx, dy, dz;
-                if (SPLINE) {
-                    const LineBasis* lb = basis + line;
-                    df sx = df_make(0.f, 0.f), sy = df_make(0.f, 0.f), sz = df_make(0.f, 0.f);
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int i = 0; i < cnt; i++) {
+        const float a = sa[i];
+        if (a == 0.0f) continue;
+        float w, cph = 1.0f, sph = 0.0f;
+        int idx;
+        if (!REF) {
+            // FP32 position relative to the origin
+            float fx, fy, fz;
+            if (SPLINE) {
+                fx = 0.f; fy = 0.f; fz = 0.f;
 #pragma unroll
-                    for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
-                        if (k <= degree) {
-                            const df bk = df_make(__ldg(&lb->hi[k]), __ldg(&lb->lo[k]));
-                            sx = df_add(sx, df_mul_f(bk, c[k].x));
-                            sy = df_add(sy, df_mul_f(bk, c[k].y));
-                            sz = df_add(sz, df_mul_f(bk, c[k].z));
-                        }
+                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                    if (k < np) {
+                        const float4 c = sp[i * np + k];
+                        fx = fmaf(bh[k], c.x, fx); fy = fmaf(bh[k], c.y, fy); fz = fmaf(bh[k], c.z, fz);
                     }
-                    dx = df_add(sx, df_make(-ox, 0.f));
-                    dy = df_add(sy, df_make(-oy, 0.f));
-                    dz = df_add(sz, df_make(-oz, 0.f));
-                } else {
-                    dx = df_diff_f(px, ox);
-                    dy = df_diff_f(py, oy);
-                    dz = df_diff_f(pz, oz);
                 }
-                const float fx = dx.hi + dx.lo, fy = dy.hi + dy.lo, fz = dz.hi + dz.lo;
-                const float dot = fmaf(fz, rz, fmaf(fy, ry, fx * rx));
-                const float l = fmaf(fz, lz, fmaf(fy, ly, fx * lx));
-                const float e = fmaf(fz, ez, fmaf(fy, ey, fx * ex));
-                df r;
-                if (p.arc) {
-                    const df r2 = df_add(df_add(df_sqr(dx), df_sqr(dy)), df_sqr(dz));
-                    r = df_sqrt(r2);
-                    if (signbit(dot)) { r.hi = -r.hi; r.lo = -r.lo; }
-                } else {
-                    r = df_add(df_add(df_mul_f(dx, rx), df_mul_f(dy, ry)), df_mul_f(dz, rz));
+                fx -= ox; fy -= oy; fz -= oz;
+            } else {
+                const float4 c = sp[i];
+                fx = c.x - ox; fy = c.y - oy; fz = c.z - oz;
+            }
+            const float l = fmaf(fz, lz, fmaf(fy, ly, fx * lx));
+            const float e = fmaf(fz, ez, fmaf(fy, ey, fx * ex));
+            float tl = 0.f, te = 0.f;
+            if (BEAM == BEAM_GAUSSIAN) {
+                w = exp2f(-fmaf(l * l, gl, e * e * ge));
+                if (fabsf(w * a) < skip_below) continue;
+            } else {
+                tl = (l - b.lf) * b.inv_dl;
+                te = (e - b.ef) * b.inv_de;
+                // outside the table by more than rounding can explain: weight 0
+                if (!(tl > -1.001f && tl < (float)(b.nl - 1) + 0.001f && te > -1.001f && te < (float)(b.ne - 1) + 0.001f))
+                    continue;
+            }
+            // exact position relative to the origin as float pairs
+            df dx, dy, dz;
+            if (SPLINE) {
+                df sx = df_make(0.f, 0.f), sy = df_make(0.f, 0.f), sz = df_make(0.f, 0.f);
+                float ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;   // accumulated low parts
+#pragma unroll
+                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                    if (k < np) {
+                        const float4 c = sp[i * np + k];
+                        const df px = two_prod(bh[k], c.x), py = two_prod(bh[k], c.y), pz = two_prod(bh[k], c.z);
+                        const df tx = two_sum(sx.hi, px.hi), ty = two_sum(sy.hi, py.hi), tz = two_sum(sz.hi, pz.hi);
+                        sx.hi = tx.hi; sy.hi = ty.hi; sz.hi = tz.hi;
+                        ex_ += tx.lo + fmaf(bl[k], c.x, px.lo);
+                        ey_ += ty.lo + fmaf(bl[k], c.y, py.lo);
+                        ez_ += tz.lo + fmaf(bl[k], c.z, pz.lo);
+                    }
                 }
+                const df ux = two_sum(sx.hi, -ox), uy = two_sum(sy.hi, -oy), uz = two_sum(sz.hi, -oz);
+                dx = fast_two_sum(ux.hi, ux.lo + ex_);
+                dy = fast_two_sum(uy.hi, uy.lo + ey_);
+                dz = fast_two_sum(uz.hi, uz.lo + ez_);
+            } else {
+                const float4 c = sp[i];
+                dx = two_sum(c.x, -ox);
+                dy = two_sum(c.y, -oy);
+                dz = two_sum(c.z, -oz);
+            }
+            const float fdx = dx.hi + dx.lo, fdy = dy.hi + dy.lo, fdz = dz.hi + dz.lo;
+            const float dot = fmaf(fdz, rz, fmaf(fdy, ry, fdx * rx));
+            float delay, rr;
+            if (p.arc) {
+                if (!pair_bin(dx, dy, dz, dot, p, &idx, &delay, &rr)) continue;
+            } else {
+                // radial coordinate = projection on the line direction
+                const df r = df_add(df_add(df_mul_f(dx, rx), df_mul_f(dy, ry)), df_mul_f(dz, rz));
+                rr = r.hi + r.lo;
                 const df t = df_mul(r, df_make(p.k_hi, p.k_lo));
-                // idx = floor(t + 0.5) decided on the pair value: with f = floor(hi)
-                // the remainder hi - f is exact, so compare (hi - f - 0.5) with -lo.
                 float f = floorf(t.hi);
-                float rem = t.hi - f;                   // exact
-                float frac_lo = t.lo;
-                if (rem + frac_lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
-                const bool up = (rem - 0.5f) >= -frac_lo;
+                float rem = t.hi - f;
+                if (rem + t.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
+                const bool up = (rem - 0.5f) >= -t.lo;
                 const float fidx = up ? f + 1.0f : f;
                 if (!(fidx >= 0.0f && fidx < (float)p.ns)) continue;
                 idx = (int)fidx;
-                if (BEAM == BEAM_GAUSSIAN) {
-                    w = exp2f(-fmaf(l * l, b.gl, e * e * b.ge));
-                } else {
-                    const float rr = r.hi + r.lo;
-                    const float tr = (rr - b.rf) * b.inv_dr;
-                    if (!(tr > -1.0f && tr < (float)(b.nr - 1))) continue;
-                    const int r0 = (int)tr;
-                    const float frr = tr < 0.0f ? 0.0f : tr - (float)r0;
-                    w = lut_weight_packed(b, r0, frr, (l - b.lf) * b.inv_dl, (e - b.ef) * b.inv_de);
-                }
-                if (p.phase_delay) {
-                    // sub-sample delay (idx - t) in samples, as a phase (CpuAlgorithm.cpp:85-92)
-                    const float dly = (up ? 1.0f : 0.0f) - rem - frac_lo;
-                    sincosf(p.two_pi_fd_over_fs * dly, &sph, &cph);
-                }
-            } else {
-                // the reference's float expressions (CpuAlgorithm.cpp:58-95 and 137-181)
-                float fx, fy, fz;
-                if (SPLINE) {
-                    const LineBasis* lb = basis + line;
-                    float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-                    for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
-                        if (k <= degree) {
-                            const float bk = __ldg(&lb->hi[k]);
-                            sx = __fadd_rn(sx, __fmul_rn(c[k].x, bk));
-                            sy = __fadd_rn(sy, __fmul_rn(c[k].y, bk));
-                            sz = __fadd_rn(sz, __fmul_rn(c[k].z, bk));
-                        }
-                    }
-                    fx = __fsub_rn(sx, ox); fy = __fsub_rn(sy, oy); fz = __fsub_rn(sz, oz);
-                } else {
-                    fx = __fsub_rn(px, ox); fy = __fsub_rn(py, oy); fz = __fsub_rn(pz, oz);
-                }
-                float r = __fadd_rn(__fadd_rn(__fmul_rn(fx, rx), __fmul_rn(fy, ry)), __fmul_rn(fz, rz));
-                const float l = __fadd_rn(__fadd_rn(__fmul_rn(fx, lx), __fmul_rn(fy, ly)), __fmul_rn(fz, lz));
-                const float e = __fadd_rn(__fadd_rn(__fmul_rn(fx, ex), __fmul_rn(fy, ey)), __fmul_rn(fz, ez));
-                if (p.arc)
-                    r = copysignf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz))), r);
-                double t;
-                if (SPLINE) {
-                    // r*2.0/(c*dt) with dt = float(1/fs) (CpuAlgorithm.cpp:161-162)
-                    const float dt = (float)(1.0 / p.fs_d);
-                    t = __ddiv_rn(__dmul_rn((double)r, 2.0), (double)__fmul_rn(p.c, dt));
-                } else {
-                    t = __ddiv_rn(__dmul_rn(__dmul_rn((double)r, 2.0), p.fs_d), p.c_d);
-                }
-                const double fidx = floor(t + 0.5);
-                if (!(fidx >= 0.0 && fidx < (double)p.ns)) continue;
-                idx = (int)fidx;
-                if (BEAM == BEAM_GAUSSIAN) w = gauss_weight_ref(b, l, e);
-                else w = lut_weight_ref(b, r, l, e);
-                if (p.phase_delay) {
-                    const float ss_delay = (float)(((double)idx - t) / p.fs_d);
-                    const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
-                    sincosf(ph, &sph, &cph);
-                }
+                delay = (up ? 1.0f : 0.0f) - rem - t.lo;
             }
-            const float amp = w * a;
-            unsigned long long* dst = bins + ((int64_t)line * p.ns + idx) * stride;
+            if (BEAM == BEAM_LUT) {
+                const float tr = (rr - b.rf) * b.inv_dr;
+                if (!(tr > -1.0f && tr < (float)(b.nr - 1))) continue;
+                const int r0 = (int)tr;
+                const float frr = tr < 0.0f ? 0.0f : tr - (float)r0;
+                w = lut_weight_packed(b, r0, frr, tl, te);
+            }
             if (p.phase_delay) {
-                bin_add(dst, amp * cph, p.scale);
-                bin_add(dst + 1, amp * sph, p.scale);
+                // sub-sample delay (idx - t) in samples as a phase (CpuAlgorithm.cpp:85-92);
+                // |argument| < pi fd/fs, where the fast sine/cosine is accurate to ~4e-7
+                __sincosf(p.two_pi_fd_over_fs * delay, &sph, &cph);
+            }
+        } else {
+            // the reference's float expressions (CpuAlgorithm.cpp:58-95 and 137-181)
+            float fx, fy, fz;
+            if (SPLINE) {
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                    if (k < np) {
+                        const float4 c = sp[i * np + k];
+                        sx = __fadd_rn(sx, __fmul_rn(c.x, bh[k]));
+                        sy = __fadd_rn(sy, __fmul_rn(c.y, bh[k]));
+                        sz = __fadd_rn(sz, __fmul_rn(c.z, bh[k]));
+                    }
+                }
+                fx = __fsub_rn(sx, ox); fy = __fsub_rn(sy, oy); fz = __fsub_rn(sz, oz);
             } else {
-                bin_add(dst, amp, p.scale);
+                const float4 c = sp[i];
+                fx = __fsub_rn(c.x, ox); fy = __fsub_rn(c.y, oy); fz = __fsub_rn(c.z, oz);
+            }
+            float r = __fadd_rn(__fadd_rn(__fmul_rn(fx, rx), __fmul_rn(fy, ry)), __fmul_rn(fz, rz));
+            const float l = __fadd_rn(__fadd_rn(__fmul_rn(fx, lx), __fmul_rn(fy, ly)), __fmul_rn(fz, lz));
+            const float e = __fadd_rn(__fadd_rn(__fmul_rn(fx, ex), __fmul_rn(fy, ey)), __fmul_rn(fz, ez));
+            if (p.arc)
+                r = copysignf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz))), r);
+            double t;
+            if (SPLINE) {
+                // r*2.0/(c*dt) with dt = float(1/fs) (CpuAlgorithm.cpp:161-162)
+                const float dt = (float)(1.0 / p.fs_d);
+                t = __ddiv_rn(__dmul_rn((double)r, 2.0), (double)__fmul_rn(p.c, dt));
+            } else {
+                t = __ddiv_rn(__dmul_rn(__dmul_rn((double)r, 2.0), p.fs_d), p.c_d);
+            }
+            const double fidx = floor(t + 0.5);
+            if (!(fidx >= 0.0 && fidx < (double)p.ns)) continue;
+            idx = (int)fidx;
+            if (BEAM == BEAM_GAUSSIAN) w = gauss_weight_ref(b, l, e);
+            else w = lut_weight_ref(b, r, l, e);
+            if (p.phase_delay) {
+                const float ss_delay = (float)(((double)idx - t) / p.fs_d);
+                const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
+                sincosf(ph, &sph, &cph);
             }
         }
+        const float amp = w * a;
+        unsigned long long* dst = lbins + (int64_t)idx * stride;
+        if (p.phase_delay) {
+            bin_add(dst, amp * cph, p.scale);
+            bin_add(dst + 1, amp * sph, p.scale);
+        } else {
+            bin_add(dst, amp, p.scale);
+        }
+    }
     }
 }
 
@@ -792,16 +887,16 @@ cudaError_t launch_project_shared(const float4* records, int64_t plane, const in
 template <int BEAM, bool SPLINE, bool REF>
 static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const float* amps, int64_t n, int degree,
                                     const uint32_t* index_list, const int* counts, int64_t list_lo,
-                                    const LineGeom* lines,
-                                    const int* line_ids, const LineTile* tiles, int num_tiles,
-                                    const LineBasis* basis, const SimParams& p, const BeamDev& b,
+                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles,
+                                    int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
                                     unsigned long long* bins, cudaStream_t stream) {
-    int64_t blocks = (n + GENERIC_THREADS - 1) / GENERIC_THREADS;
-    if (blocks > 1184) blocks = 1184;   // grid-stride beyond 8 waves of 152 SMs
-    if (index_list) blocks = 4;         // the near-origin residue is a handful of scatterers
-    if (blocks < 1) blocks = 1;
-    dim3 grid((unsigned)blocks, (unsigned)num_tiles);
-    project_generic_kernel<BEAM, SPLINE, REF><<<grid, GENERIC_THREADS, 0, stream>>>(
+    // chunks over all scatterers (for the residue list: over n, the kernel
+    // returns early past the list length, which is a handful)
+    int64_t chunks = (n + PAIR_CHUNK - 1) / PAIR_CHUNK;
+    if (index_list) chunks = 8;
+    if (chunks < 1) chunks = 1;
+    dim3 grid((unsigned)chunks, (unsigned)num_tiles);
+    project_generic_kernel<BEAM, SPLINE, REF><<<grid, PAIR_THREADS, 0, stream>>>(
         xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b);
     return cudaGetLastError();
 }
