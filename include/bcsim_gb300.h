@@ -141,6 +141,32 @@ int bcsim_get_debug_data(const bcsim_handle* h, const char* key, double* out, in
 typedef void (*bcsim_log_fn)(int level, const char* message, void* user);
 int bcsim_set_logger(bcsim_handle* h, bcsim_log_fn fn, void* user);
 
+/* Allocation-free simulation (no counterpart in the reference).
+ *
+ * For callers that cannot allocate GPU memory -- pipelines that reserve all
+ * device memory once at start-up, processes whose device memory belongs to
+ * another framework's pool -- this one call simulates fixed scatterers with an
+ * analytic Gaussian beam without allocating anything on the device: the caller
+ * passes the scatterers d_xyza (device, float4 [n] = x, y, z, amplitude) and the
+ * output d_out (device, complex64 [num_lines][ceil(ns / radial_decimation)]);
+ * the scan lines and excitation are host arrays as in bcsim_set_scan_sequence /
+ * bcsim_set_excitation.  All intermediates live in one static device array of
+ * 32 MiB that every GPU loading this library holds until exit.  Limits:
+ * num_lines <= 4096, num_lines * ns * (phase_delay ? 2 : 1) <= 3932160,
+ * ns + num_samples - 1 <= 65536.  amplitude_sum_bound must bound sum |a|
+ * (it sets the fixed-point scale of the bins).  The first call on each device
+ * looks up the static array's address (make it before any stream capture).
+ * Calls share the array: calls that overlap on the GPU race, so issue them on
+ * one stream.  Returns when the IQ is in d_out; on failure a message is written
+ * to err (err_cap bytes). */
+int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const float* origins, const float* directions,
+                                 const float* lateral_dirs, int num_lines, float line_length, float sound_speed,
+                                 const float* samples, int num_samples, int center_index, float sampling_frequency,
+                                 float demod_freq, float sigma_lateral, float sigma_elevational,
+                                 int use_arc_projection, int phase_delay, int radial_decimation,
+                                 float amplitude_sum_bound, void* d_out, int64_t cap_complex, void* stream,
+                                 char* err, int err_cap);
+
 #ifdef __cplusplus
 }
 #endif

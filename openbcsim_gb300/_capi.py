@@ -42,6 +42,10 @@ SIGNATURES = [
     ("bcsim_get_stream", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bcsim_get_debug_data", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64, _i64p]),
     ("bcsim_set_logger", C.c_int, [C.c_void_p, LOG_FN, C.c_void_p]),
+    ("bcsim_simulate_fixed_noalloc", C.c_int,
+     [C.c_void_p, C.c_int64, _f32p, _f32p, _f32p, C.c_int, C.c_float, C.c_float, _f32p, C.c_int, C.c_int,
+      C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_int64,
+      C.c_void_p, C.c_char_p, C.c_int]),
 ]
 
 _lib = None
