@@ -173,6 +173,9 @@ def run_gpu(args):
     sim = gb.RfSimulator("gpu")
     sim.set_parameter("gpu_device", str(local))
     gb.configure_job(sim, job)
+    # every timed step redoes the whole pipeline, including the per-scatterer
+    # distance/bin/phase pass and the sort (no reuse of records between steps)
+    sim.set_parameter("record_cache", "off")
     apply_params(sim, args.param)
     sim.set_parameter("store_kernel_details", "on")
     L, nd = sim.output_shape()

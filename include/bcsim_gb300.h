@@ -36,6 +36,7 @@ extern "C" {
 #define BCSIM_E_CAPACITY      4   /* caller buffer too small                         */
 #define BCSIM_E_MEMORY        5   /* device/host allocation refused                  */
 #define BCSIM_E_INTERNAL      6   /* internal invariant (std::logic_error)           */
+#define BCSIM_E_PENDING       7   /* request not finished within the wait timeout    */
 
 typedef struct bcsim_handle bcsim_handle;
 
@@ -140,6 +141,58 @@ int bcsim_get_debug_data(const bcsim_handle* h, const char* key, double* out, in
  * 3 FATAL).  fn = NULL restores the silent default (DummyLog). */
 typedef void (*bcsim_log_fn)(int level, const char* message, void* user);
 int bcsim_set_logger(bcsim_handle* h, bcsim_log_fn fn, void* user);
+
+/* ---------------------------------------------------------------------------
+ * Batched simulation (the reference has none: its GPU algorithm runs one
+ * simulation per simulate_lines call, one line at a time, GpuAlgorithm.cpp:189-265).
+ * A batch groups configured handles; running it prepares every handle, then
+ * submits all of their device work at once, each handle on its own stream, and
+ * from the second unchanged run on replays that submission as one captured CUDA
+ * graph.  Results are identical to each handle's own bcsim_simulate_lines.
+ * ------------------------------------------------------------------------- */
+typedef struct bcsim_batch bcsim_batch;
+int bcsim_batch_create(bcsim_handle* const* handles, int count, int use_graph, bcsim_batch** out);
+int bcsim_batch_destroy(bcsim_batch* b);
+const char* bcsim_batch_last_error(const bcsim_batch* b);
+/* Run all jobs; host_outs[i] (may be NULL) receives job i's IQ (caps[i] complex
+ * values), as bcsim_simulate_lines would.  Blocks until done. */
+int bcsim_batch_run(bcsim_batch* b, float* const* host_outs, const int64_t* caps);
+/* Run all jobs into device buffers without waiting; *stream (if not NULL)
+ * receives the stream that completes when every job is done. */
+int bcsim_batch_run_device(bcsim_batch* b, void* const* device_outs, const int64_t* caps, void** stream);
+
+/* ---------------------------------------------------------------------------
+ * Request server (no counterpart in the reference, whose callers run one
+ * simulate_lines at a time, e.g. src/qt5gui/MainWindow.cpp:656-735).
+ * Phantoms -- configured handles: parameters, excitation, beam, scatterers --
+ * are copied once and stay resident on the device.  Each request asks for
+ * scan lines of one phantom.  A worker thread admits requests in arrival order
+ * as simulator slots of their phantom free up, creating up to
+ * max_slots_per_phantom slots while the device-memory budget allows, and runs
+ * admitted requests concurrently on separate streams (continuous batching).
+ * A request's IQ is identical to bcsim_simulate_lines of its phantom with its
+ * lines, whatever else is in flight.
+ * ------------------------------------------------------------------------- */
+typedef struct bcsim_server bcsim_server;
+int bcsim_server_create(int64_t hbm_budget_bytes, int max_slots_per_phantom, bcsim_server** out);
+int bcsim_server_destroy(bcsim_server* s);
+const char* bcsim_server_last_error(const bcsim_server* s);
+/* Copies the configuration and scatterers of a configured handle; *phantom_id
+ * identifies it in requests.  The handle stays the caller's. */
+int bcsim_server_add_phantom(bcsim_server* s, bcsim_handle* configured, int* phantom_id);
+/* Queues a request; returns at once with its id. */
+int bcsim_server_submit(bcsim_server* s, int phantom_id, const float* origins, const float* directions,
+                        const float* lateral_dirs, const float* timestamps, int num_lines, float line_length,
+                        int radial_decimation, int64_t* request_id);
+/* Waits up to timeout_ms (-1: no limit) for a request; BCSIM_E_PENDING if not
+ * done.  On success copies the IQ (complex64 [num_lines][num_samples]) into out
+ * and releases the request; latency_ms = submit to result on the host. */
+int bcsim_server_wait(bcsim_server* s, int64_t request_id, float* out, int64_t cap_complex, int64_t* num_lines,
+                      int64_t* num_samples, double* latency_ms, int timeout_ms);
+/* Counters: completed and failed requests, latency percentiles over completed
+ * requests, projections done, device bytes held by slots, queued requests. */
+int bcsim_server_stats(bcsim_server* s, int64_t* completed, int64_t* failed, double* p50_ms, double* p99_ms,
+                       int64_t* projections, int64_t* hbm_in_use, int64_t* queue_depth);
 
 /* Allocation-free simulation (no counterpart in the reference).
  *

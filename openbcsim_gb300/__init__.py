@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _capi
 
-__all__ = ["RfSimulator", "SimulatorError", "load_library"]
+__all__ = ["RfSimulator", "Batch", "Server", "SimulatorError", "load_library", "configure_job"]
 
 
 class SimulatorError(RuntimeError):
@@ -224,3 +224,105 @@ def configure_job(sim: RfSimulator, job, precision_mode: str = "fp64"):
     for sp in job.splines:
         sim.add_spline_scatterers(sp.degree, sp.knots, sp.control_points, sp.amplitudes)
     return sim
+
+
+class Batch:
+    """Several configured simulators run together (include/bcsim_gb300.h,
+    bcsim_batch_*): all of their device work is submitted at once on separate
+    streams and, from the second unchanged run on, replayed as one CUDA graph."""
+
+    def __init__(self, sims, use_graph: bool = True):
+        self._lib = _capi.load()
+        self._sims = list(sims)
+        arr = (C.c_void_p * len(self._sims))(*[s.handle.value for s in self._sims])
+        b = C.c_void_p()
+        rc = self._lib.bcsim_batch_create(arr, len(self._sims), int(use_graph), C.byref(b))
+        if rc != 0:
+            raise SimulatorError(rc, "bcsim_batch_create failed")
+        self._b = b
+
+    def __del__(self):
+        b = getattr(self, "_b", None)
+        if b is not None and b.value:
+            self._lib.bcsim_batch_destroy(b)
+            self._b = None
+
+    def run(self, outputs=None):
+        """Run every job; returns (or fills) one [lines, samples] complex64 array per job."""
+        if outputs is None:
+            outputs = [np.empty(s.output_shape(), np.complex64) for s in self._sims]
+        ptrs = (C.c_void_p * len(outputs))(*[o.ctypes.data for o in outputs])
+        caps = (C.c_int64 * len(outputs))(*[o.size for o in outputs])
+        rc = self._lib.bcsim_batch_run(self._b, ptrs, caps)
+        if rc != 0:
+            raise SimulatorError(rc, self._lib.bcsim_batch_last_error(self._b).decode())
+        return outputs
+
+    def run_device(self, device_ptrs, capacities) -> int:
+        """Run into device buffers without waiting; returns the completion stream."""
+        ptrs = (C.c_void_p * len(device_ptrs))(*device_ptrs)
+        caps = (C.c_int64 * len(capacities))(*capacities)
+        st = C.c_void_p()
+        rc = self._lib.bcsim_batch_run_device(self._b, ptrs, caps, C.byref(st))
+        if rc != 0:
+            raise SimulatorError(rc, self._lib.bcsim_batch_last_error(self._b).decode())
+        return st.value or 0
+
+
+class Server:
+    """Continuous-batching request server over resident phantoms
+    (include/bcsim_gb300.h, bcsim_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int = 16 << 30, max_slots_per_phantom: int = 4):
+        self._lib = _capi.load()
+        s = C.c_void_p()
+        rc = self._lib.bcsim_server_create(int(hbm_budget_bytes), int(max_slots_per_phantom), C.byref(s))
+        if rc != 0:
+            raise SimulatorError(rc, "bcsim_server_create failed")
+        self._s = s
+        self._shapes = {}
+
+    def close(self):
+        s = getattr(self, "_s", None)
+        if s is not None and s.value:
+            self._lib.bcsim_server_destroy(s)
+            self._s = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise SimulatorError(rc, self._lib.bcsim_server_last_error(self._s).decode())
+
+    def add_phantom(self, sim: RfSimulator) -> int:
+        pid = C.c_int()
+        self._check(self._lib.bcsim_server_add_phantom(self._s, sim.handle, C.byref(pid)))
+        return pid.value
+
+    def submit(self, phantom: int, origins, directions, line_length, lateral_dirs, timestamps, decimation: int) -> int:
+        o, d, l, t = (np.ascontiguousarray(x, np.float32) for x in (origins, directions, lateral_dirs, timestamps))
+        rid = C.c_int64()
+        self._check(self._lib.bcsim_server_submit(self._s, int(phantom), _ptr(o), _ptr(d), _ptr(l), _ptr(t),
+                                                  o.shape[0], float(line_length), int(decimation), C.byref(rid)))
+        self._shapes[rid.value] = o.shape[0]
+        return rid.value
+
+    def wait(self, request_id: int, max_samples: int = 1 << 16, timeout_ms: int = -1):
+        """(IQ [lines, samples] complex64, latency in ms) of a finished request."""
+        L = self._shapes.get(request_id, 1)
+        buf = np.empty(L * max_samples, np.complex64)
+        nl, nd, lat = C.c_int64(), C.c_int64(), C.c_double()
+        rc = self._lib.bcsim_server_wait(self._s, int(request_id), buf.ctypes.data_as(C.POINTER(C.c_float)),
+                                         buf.size, C.byref(nl), C.byref(nd), C.byref(lat), int(timeout_ms))
+        self._check(rc)
+        self._shapes.pop(request_id, None)
+        return buf[: nl.value * nd.value].reshape(nl.value, nd.value).copy(), lat.value
+
+    def stats(self) -> dict:
+        c, f, q, pr, hb, qd = (C.c_int64() for _ in range(6))
+        p50, p99 = C.c_double(), C.c_double()
+        self._check(self._lib.bcsim_server_stats(self._s, C.byref(c), C.byref(f), C.byref(p50), C.byref(p99),
+                                                 C.byref(pr), C.byref(hb), C.byref(qd)))
+        return {"completed": c.value, "failed": f.value, "p50_ms": p50.value, "p99_ms": p99.value,
+                "projections": pr.value, "hbm_in_use": hb.value, "queue_depth": qd.value}

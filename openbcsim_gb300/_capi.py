@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libbcsim_gb300.so")
 
 OK = 0
-E_INVALID, E_NOT_CONFIGURED, E_CUDA, E_CAPACITY, E_MEMORY, E_INTERNAL = 1, 2, 3, 4, 5, 6
+E_INVALID, E_NOT_CONFIGURED, E_CUDA, E_CAPACITY, E_MEMORY, E_INTERNAL, E_PENDING = 1, 2, 3, 4, 5, 6, 7
 
 # every symbol the header declares: (name, restype, argtypes)
 _f32p = C.POINTER(C.c_float)
@@ -42,6 +42,21 @@ SIGNATURES = [
     ("bcsim_get_stream", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bcsim_get_debug_data", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64, _i64p]),
     ("bcsim_set_logger", C.c_int, [C.c_void_p, LOG_FN, C.c_void_p]),
+    ("bcsim_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    ("bcsim_batch_destroy", C.c_int, [C.c_void_p]),
+    ("bcsim_batch_last_error", C.c_char_p, [C.c_void_p]),
+    ("bcsim_batch_run", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _i64p]),
+    ("bcsim_batch_run_device", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _i64p, C.POINTER(C.c_void_p)]),
+    ("bcsim_server_create", C.c_int, [C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
+    ("bcsim_server_destroy", C.c_int, [C.c_void_p]),
+    ("bcsim_server_last_error", C.c_char_p, [C.c_void_p]),
+    ("bcsim_server_add_phantom", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    ("bcsim_server_submit", C.c_int, [C.c_void_p, C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float, C.c_int,
+                                      _i64p]),
+    ("bcsim_server_wait", C.c_int, [C.c_void_p, C.c_int64, _f32p, C.c_int64, _i64p, _i64p,
+                                    C.POINTER(C.c_double), C.c_int]),
+    ("bcsim_server_stats", C.c_int, [C.c_void_p, _i64p, _i64p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     _i64p, _i64p, _i64p]),
     ("bcsim_simulate_fixed_noalloc", C.c_int,
      [C.c_void_p, C.c_int64, _f32p, _f32p, _f32p, C.c_int, C.c_float, C.c_float, _f32p, C.c_int, C.c_int,
       C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_int64,

@@ -22,10 +22,10 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 
 CU_SOURCES = ["project.cu", "conv.cu", "noalloc.cu"]
-CPP_SOURCES = ["engine.cpp", "host_dsp.cpp", "capi.cpp"]
+CPP_SOURCES = ["engine.cpp", "host_dsp.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
 HEADERS = ["kernels.hpp", "dfloat.cuh", "engine.hpp", "host_dsp.hpp"]
 
-HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-Wall", "-Wno-unused-function"]
+HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-Wall", "-Wno-unused-function", "-pthread"]
 
 
 def _newer(src_list, target):
@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(m)
     objs = [o for o, _ in results]
     if force or _newer(objs, LIB):
-        cmd = [NVCC, "-shared", "-o", LIB, *objs, *ARCH, "-Xcompiler", "-fPIC"]
+        cmd = [NVCC, "-shared", "-o", LIB, *objs, *ARCH, "-Xcompiler", "-fPIC", "-lpthread"]
         out = subprocess.run(cmd, capture_output=True, text=True)
         if out.returncode != 0:
             raise RuntimeError("link failed: " + " ".join(cmd) + "\n" + out.stdout + out.stderr)

@@ -1,0 +1,202 @@
+// batch.cpp -- many simulations in one submission.
+//
+// A batch holds configured simulators.  Running it prepares every simulator on
+// the host (cached per configuration), then enqueues all of their device work
+// at once, each simulator on its own stream so that small and large jobs
+// overlap on the GPU, joined back into one origin stream.  From the second run
+// with unchanged configurations on, that whole multi-stream submission is
+// replayed as one captured CUDA graph, so a batch of many small jobs costs one
+// graph launch instead of tens of kernel launches per job.
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bcsim_gb300.h"
+#include "engine.hpp"
+
+struct bcsim_handle;   // defined in capi.cpp
+namespace bcsim_gb300 {
+Simulator& simulator_of(bcsim_handle* h);
+}
+
+using bcsim_gb300::SimError;
+using bcsim_gb300::Simulator;
+
+struct bcsim_batch {
+    std::vector<bcsim_handle*> handles;
+    bool use_graph = true;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> versions;   // configurations the graph was captured for
+    std::vector<void*> outs;          // outputs the graph writes
+    int runs_since_change = 0;
+    std::string last_error;
+
+    ~bcsim_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto e : joins) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (origin) cudaStreamDestroy(origin);
+    }
+};
+
+namespace {
+
+#define BATCH_CUDA(call)                                                                          \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) throw SimError(BCSIM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void enqueue_all(bcsim_batch* b, const std::vector<float2*>& outs) {
+    BATCH_CUDA(cudaEventRecord(b->fork, b->origin));
+    for (size_t i = 0; i < b->handles.size(); i++) {
+        Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+        cudaStream_t st = s.stream();
+        BATCH_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
+        s.enqueue(st, outs[i], false);
+        BATCH_CUDA(cudaEventRecord(b->joins[i], st));
+        BATCH_CUDA(cudaStreamWaitEvent(b->origin, b->joins[i], 0));
+    }
+}
+
+void run(bcsim_batch* b, const std::vector<float2*>& outs) {
+    const size_t n = b->handles.size();
+    std::vector<uint64_t> versions(n);
+    for (size_t i = 0; i < n; i++) {
+        Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+        s.prepare();
+        versions[i] = s.config_version();
+    }
+    std::vector<void*> outv(outs.begin(), outs.end());
+    const bool same = versions == b->versions && outv == b->outs;
+    if (!same) {
+        b->versions = versions;
+        b->outs = outv;
+        b->runs_since_change = 0;
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+    }
+    // the first run after a change is submitted directly: it also produces the
+    // records the later (captured) runs reuse
+    if (!b->use_graph || b->runs_since_change == 0) {
+        enqueue_all(b, outs);
+        b->runs_since_change++;
+        return;
+    }
+    if (!b->exec) {
+        cudaGraph_t graph = nullptr;
+        BATCH_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed));
+        try {
+            enqueue_all(b, outs);
+        } catch (...) {
+            cudaStreamEndCapture(b->origin, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        BATCH_CUDA(cudaStreamEndCapture(b->origin, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&b->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw SimError(BCSIM_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    }
+    BATCH_CUDA(cudaGraphLaunch(b->exec, b->origin));
+    b->runs_since_change++;
+}
+
+template <typename F>
+int guarded(bcsim_batch* b, F&& f) {
+    if (!b) return BCSIM_E_INVALID;
+    try {
+        f();
+        b->last_error.clear();
+        return BCSIM_OK;
+    } catch (const SimError& e) {
+        b->last_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        b->last_error = e.what();
+        return BCSIM_E_INTERNAL;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bcsim_batch_create(bcsim_handle* const* handles, int count, int use_graph, bcsim_batch** out) {
+    if (!out || count < 0 || (count > 0 && !handles)) return BCSIM_E_INVALID;
+    *out = nullptr;
+    bcsim_batch* b = new bcsim_batch();
+    b->handles.assign(handles, handles + count);
+    b->use_graph = use_graph != 0;
+    const int rc = guarded(b, [&] {
+        for (auto h : b->handles)
+            if (!h) throw SimError(BCSIM_E_INVALID, "null handle in batch");
+        if (count > 0) bcsim_gb300::simulator_of(b->handles[0]).stream();   // device ready
+        BATCH_CUDA(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
+        BATCH_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        b->joins.resize(count);
+        for (auto& e : b->joins) BATCH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    });
+    if (rc != BCSIM_OK) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return BCSIM_OK;
+}
+
+int bcsim_batch_destroy(bcsim_batch* b) {
+    delete b;
+    return BCSIM_OK;
+}
+
+const char* bcsim_batch_last_error(const bcsim_batch* b) { return b ? b->last_error.c_str() : "null batch"; }
+
+int bcsim_batch_run(bcsim_batch* b, float* const* host_outs, const int64_t* caps) {
+    return guarded(b, [&] {
+        const size_t n = b->handles.size();
+        std::vector<float2*> outs(n);
+        for (size_t i = 0; i < n; i++) {
+            Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+            s.prepare();
+            if (host_outs && host_outs[i] && caps && caps[i] < s.num_lines() * s.num_out_samples())
+                throw SimError(BCSIM_E_CAPACITY, "output buffer too small for job " + std::to_string(i));
+            outs[i] = s.internal_output();
+        }
+        run(b, outs);
+        if (host_outs) {
+            for (size_t i = 0; i < n; i++) {
+                if (!host_outs[i]) continue;
+                Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+                BATCH_CUDA(cudaMemcpyAsync(host_outs[i], outs[i], (size_t)s.num_lines() * s.num_out_samples() * sizeof(float2),
+                                           cudaMemcpyDeviceToHost, b->origin));
+            }
+        }
+        BATCH_CUDA(cudaStreamSynchronize(b->origin));
+        for (size_t i = 0; i < n; i++) bcsim_gb300::simulator_of(b->handles[i]).check_device_flag();
+    });
+}
+
+int bcsim_batch_run_device(bcsim_batch* b, void* const* device_outs, const int64_t* caps, void** stream) {
+    return guarded(b, [&] {
+        const size_t n = b->handles.size();
+        std::vector<float2*> outs(n);
+        for (size_t i = 0; i < n; i++) {
+            Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+            s.prepare();
+            if (!device_outs || !device_outs[i] || !caps || caps[i] < s.num_lines() * s.num_out_samples())
+                throw SimError(BCSIM_E_CAPACITY, "device output missing or too small for job " + std::to_string(i));
+            outs[i] = static_cast<float2*>(device_outs[i]);
+        }
+        run(b, outs);
+        if (stream) *stream = (void*)b->origin;
+    });
+}
+
+}  // extern "C"

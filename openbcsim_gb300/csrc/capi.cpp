@@ -18,6 +18,10 @@ struct bcsim_handle {
     std::string last_error;
 };
 
+namespace bcsim_gb300 {
+Simulator& simulator_of(bcsim_handle* h) { return h->sim; }
+}  // namespace bcsim_gb300
+
 namespace {
 template <typename F>
 int guarded(bcsim_handle* h, F&& f) {

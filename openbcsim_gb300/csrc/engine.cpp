@@ -6,6 +6,8 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <map>
+#include <mutex>
 #include <sstream>
 
 #include "../../include/bcsim_gb300.h"
@@ -112,6 +114,7 @@ cudaStream_t Simulator::stream() {
 // ---------------------------------------------------------------------------
 void Simulator::set_parameter(const std::string& key, const std::string& value) {
     bool b = false;
+    cfg_version_++;
     if (key == "verbose") {
         verbose_ = std::stoi(value);
     } else if (key == "sound_speed") {
@@ -164,6 +167,12 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
         if (!(v >= 0.0 && v < 1.0)) throw SimError(BCSIM_E_INVALID, "fir_tail_energy must be in [0, 1)");
         if (v != fir_tail_) tables_valid_ = false;
         fir_tail_ = v;
+    } else if (key == "record_cache") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        record_cache_ = b;
+    } else if (key == "autotune") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        autotune_ = b;
     } else if (key == "cull") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         cull_ = b;
@@ -201,6 +210,8 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "fir_tail_energy") return fmt_double(fir_tail_);
     if (key == "tile_lines") return std::to_string(tile_lines_);
     if (key == "cull") return cull_ ? "on" : "off";
+    if (key == "record_cache") return record_cache_ ? "on" : "off";
+    if (key == "autotune") return autotune_ ? "on" : "off";
     if (key == "fir_taps") return std::to_string(tap_count_);
     throw SimError(BCSIM_E_INVALID, "Illegal key: " + key);
 }
@@ -209,6 +220,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
 // configuration
 // ---------------------------------------------------------------------------
 void Simulator::set_excitation(const float* samples, int n, int center_index, float fs, float demod_freq) {
+    cfg_version_++;
     if (n < 0 || (n > 0 && !samples)) throw SimError(BCSIM_E_INVALID, "set_excitation: invalid samples");
     taps_.assign(samples, samples + n);
     center_ = center_index;
@@ -259,9 +271,11 @@ void Simulator::set_scan_sequence(const float* origins, const float* dirs, const
     scan_set_ = true;
     lines_valid_ = false;
     tables_valid_ = false;
+    cfg_version_++;
 }
 
 void Simulator::set_analytical_profile(float sigma_lateral, float sigma_elevational) {
+    cfg_version_++;
     log(1, "Setting analytical beam profile for GPU algorithm");
     beam_type_ = BEAM_GAUSSIAN;
     sigma_l_ = sigma_lateral;
@@ -284,9 +298,12 @@ void Simulator::set_lookup_profile(const float* samples, int nr, int nl, int ne,
     for (float v : lut_) lut_absmax_ = std::max(lut_absmax_, (double)std::fabs(v));
     beam_type_ = BEAM_LUT;
     lut_uploaded_ = false;
+    cfg_version_++;
 }
 
 void Simulator::clear_fixed_scatterers() {
+    cfg_version_++;
+    data_version_++;
     fixed_n_ = 0;
     num_fixed_sets_ = 0;
     fixed_sum_abs_ = 0.0;
@@ -321,10 +338,16 @@ void Simulator::add_fixed_scatterers(const float* xyza, int64_t n) {
     }
     fixed_n_ += n;
     num_fixed_sets_ += 1;
+    cfg_version_++;
+    data_version_++;
     if (verbose_) log(1, "Number of fixed scatterers: " + std::to_string(fixed_n_));
 }
 
-void Simulator::clear_spline_scatterers() { splines_.clear(); }
+void Simulator::clear_spline_scatterers() {
+    splines_.clear();
+    cfg_version_++;
+    data_version_++;
+}
 
 void Simulator::add_spline_scatterers(int degree, const float* knots, int num_knots, const float* cps,
                                       const float* amps, int64_t n, int num_cs) {
@@ -362,6 +385,8 @@ void Simulator::add_spline_scatterers(int degree, const float* knots, int num_kn
         }
     }
     splines_.push_back(std::move(ds));
+    cfg_version_++;
+    data_version_++;
     if (verbose_) log(1, "Number of spline datasets: " + std::to_string(splines_.size()));
 }
 
@@ -565,23 +590,26 @@ struct EventTimer {
 };
 }  // namespace
 
-void Simulator::simulate(float2* dev_out, float* host_out) {
+// ---------------------------------------------------------------------------
+// prepare: everything the host computes or uploads for one configuration
+// ---------------------------------------------------------------------------
+void Simulator::prepare() {
     throw_if_not_configured();
     if (amplitude_nonfinite_) throw SimError(BCSIM_E_INVALID, "Nan in scatterer projection.");
     ensure_device();
+    if (plan_.version == cfg_version_) return;
     const cudaStream_t st = stream_;
     const int L = num_lines_;
-    const int ns = (int)ns_;
     if (ns_ <= 0) throw SimError(BCSIM_E_INVALID, "line length gives no RF samples");
     if (ns_ >= (int64_t)1 << 30) throw SimError(BCSIM_E_INVALID, "too many RF samples per line");
+    const int ns = (int)ns_;
     prepare_excitation_tables();
     prepare_lines();
-    if (store_details_) debug_.clear();
-    EventTimer total(store_details_, st);
-    EventTimer timer(store_details_, st);
+    Plan& P = plan_;
+    P = Plan();
 
     // beam
-    BeamDev b;
+    BeamDev& b = P.b;
     std::memset(&b, 0, sizeof(b));
     b.type = beam_type_;
     if (beam_type_ == BEAM_GAUSSIAN) {
@@ -617,7 +645,7 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     }
 
     // simulation constants
-    SimParams p;
+    SimParams& p = P.p;
     std::memset(&p, 0, sizeof(p));
     p.ns = ns;
     p.num_lines = L;
@@ -654,27 +682,15 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
         p.cull_r2 = (float)(r * r);
     }
 
-    const int stride = phase_delay_ ? 2 : 1;
-    const size_t bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
-    bins_.reserve(bins_bytes);
-    timer.restart();
-    BCSIM_CUDA(cudaMemsetAsync(bins_.get(), 0, bins_bytes, st));
-    if (store_details_) debug_["kernel_memset_ms"].push_back(timer.stop());
-    unsigned long long* bins = bins_.as<unsigned long long>();
-    const LineGeom* lines_d = lines_dev_.as<LineGeom>();
-
     // per-line spline knot intervals and basis (CpuAlgorithm.cpp:101-133)
-    struct SplineLines {
-        std::vector<int> mu;
-        std::vector<LineBasis> basis;
-    };
-    std::vector<SplineLines> spl(splines_.size());
+    std::vector<std::vector<int>> mus(splines_.size());
+    std::vector<std::vector<LineBasis>> bases(splines_.size());
     for (size_t d = 0; d < splines_.size(); d++) {
         const SplineDataset& ds = splines_[d];
         if (ds.n == 0) continue;
         if (ds.num_cs <= ds.degree) throw SimError(BCSIM_E_INVALID, "too few spline control points for given degree");
-        spl[d].mu.resize(L);
-        spl[d].basis.resize(L);
+        mus[d].resize(L);
+        bases[d].resize(L);
         for (int i = 0; i < L; i++) {
             const float t = timestamps_[i];
             const int mu = knot_interval(ds.knots, t);
@@ -696,26 +712,25 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
                     lb.lo[j - lo] = mode_ == MODE_FP64 ? (float)(v - (double)hi) : 0.0f;
                 }
             }
-            spl[d].mu[i] = mu;
-            spl[d].basis[i] = lb;
+            mus[d][i] = mu;
+            bases[d][i] = lb;
         }
     }
 
-    const bool shared = shared_origin_ && arc_;
+    P.shared = shared_origin_ && arc_;
     // splines go through the shared path when every line sees them at one time
-    std::vector<char> spline_shared(splines_.size(), 0);
-    int64_t n_shared = shared ? fixed_n_ : 0;
-    if (shared && timestamps_equal_) {
+    P.spline_shared.assign(splines_.size(), 0);
+    P.n_shared = P.shared ? fixed_n_ : 0;
+    if (P.shared && timestamps_equal_) {
         for (size_t d = 0; d < splines_.size(); d++) {
             if (splines_[d].n > 0) {
-                spline_shared[d] = 1;
-                n_shared += splines_[d].n;
+                P.spline_shared[d] = 1;
+                P.n_shared += splines_[d].n;
             }
         }
     }
 
-    // line tiles for the per-pair kernel
-    // lines of a tile: same knot interval (splines), nearby directions
+    // lines of a per-pair tile: same knot interval (splines), nearby directions
     auto make_tiles = [&](const std::vector<int>* mu, std::vector<int>& ids, std::vector<LineTile>& tiles) {
         ids.resize(L);
         std::iota(ids.begin(), ids.end(), 0);
@@ -738,35 +753,26 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
             i = j;
         }
     };
-    // upload tiles/ids/basis for all per-pair launches at once (one region per launch)
-    struct GenLaunch {
-        int kind;          // 0 fixed, 1 spline dataset
-        int d;
-        size_t tile_off, num_tiles, id_off, basis_off;
-    };
-    std::vector<GenLaunch> gl;
     std::vector<LineTile> all_tiles;
     std::vector<int> all_ids;
     std::vector<LineBasis> all_basis;
     auto add_gen = [&](int kind, int d) {
         std::vector<int> ids;
         std::vector<LineTile> tiles;
-        make_tiles(kind == 1 ? &spl[d].mu : nullptr, ids, tiles);
+        make_tiles(kind == 1 ? &mus[d] : nullptr, ids, tiles);
         GenLaunch g;
         g.kind = kind;
         g.d = d;
         g.tile_off = all_tiles.size();
         g.num_tiles = tiles.size();
-        g.id_off = all_ids.size();
         g.basis_off = all_basis.size();
-        for (auto& t : tiles) t.first += (int)g.id_off;
+        const size_t id_off = all_ids.size();
+        for (auto& t : tiles) t.first += (int)id_off;
         all_tiles.insert(all_tiles.end(), tiles.begin(), tiles.end());
         all_ids.insert(all_ids.end(), ids.begin(), ids.end());
-        if (kind == 1) all_basis.insert(all_basis.end(), spl[d].basis.begin(), spl[d].basis.end());
-        gl.push_back(g);
+        if (kind == 1) all_basis.insert(all_basis.end(), bases[d].begin(), bases[d].end());
+        P.gl.push_back(g);
     };
-    // generic fixed: when lines do not share an origin (or arc projection is off);
-    // with a shared origin only the near-origin residue goes per pair
     if (fixed_n_ > 0) add_gen(0, -1);
     for (size_t d = 0; d < splines_.size(); d++)
         if (splines_[d].n > 0) add_gen(1, (int)d);
@@ -780,11 +786,15 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     if (!all_basis.empty())
         BCSIM_CUDA(cudaMemcpyAsync(gen_basis_.get(), all_basis.data(), all_basis.size() * sizeof(LineBasis), cudaMemcpyHostToDevice, st));
 
-    // ---------------- shared-origin path ----------------
+    // device buffers
+    const int stride = phase_delay_ ? 2 : 1;
+    P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
+    bins_.reserve(P.bins_bytes);
     counts_.reserve(4 * sizeof(int));
-    if (n_shared > 0) {
-        timer.restart();
-        const int64_t N = n_shared;
+    out_.reserve((size_t)L * nd_ * sizeof(float2));
+    P.spline_off.assign(splines_.size(), -1);
+    if (P.n_shared > 0) {
+        const int64_t N = P.n_shared;
         keys_in_.reserve(N * sizeof(uint32_t));
         vals_in_.reserve(N * sizeof(uint32_t));
         keys_out_.reserve(N * sizeof(uint32_t));
@@ -792,94 +802,133 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
         recA_.reserve(N * sizeof(float4));
         recB_.reserve(N * sizeof(float4));
         records_.reserve((size_t)N * 2 * sizeof(float4));
-        const float* origin = lines_[0].o;
-        int64_t off = 0;
-        if (fixed_n_ > 0) {
-            BCSIM_CUDA(launch_prep_shared(fixed_xyza_.as<float4>(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
-                                          vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
-            off = fixed_n_;
-        }
-        std::vector<int64_t> spline_off(splines_.size(), -1);
-        std::vector<double> bd;
-        std::vector<float> bf;
+        int64_t off = fixed_n_;
+        std::vector<double> bd(64 * std::max<size_t>(1, splines_.size()), 0.0);
+        std::vector<float> bf(64 * std::max<size_t>(1, splines_.size()), 0.0f);
         for (size_t d = 0; d < splines_.size(); d++) {
-            if (!spline_shared[d]) continue;
+            if (!P.spline_shared[d]) continue;
             const SplineDataset& ds = splines_[d];
-            const LineBasis& lb = spl[d].basis[0];
-            bd.clear(); bf.clear();
+            const int lo = mus[d][0] - ds.degree;
             for (int k2 = 0; k2 <= ds.degree; k2++) {
-                bd.push_back((double)lb.hi[k2] + (double)lb.lo[k2]);
-                bf.push_back(lb.hi[k2]);
+                // exact double basis for the render (bit parity with the FP64 oracle)
+                bd[64 * d + k2] = bspline_basis_d(lo + k2, ds.degree, (double)timestamps_[0], ds.knots);
+                bf[64 * d + k2] = bases[d][0].hi[k2];
             }
-            // exact double basis for the render (the pair above is exact to ~48 bits;
-            // recompute in double for bit parity with the FP64 oracle)
-            if (mode_ == MODE_FP64) {
-                const int lo = spl[d].mu[0] - ds.degree;
-                for (int k2 = 0; k2 <= ds.degree; k2++) bd[k2] = bspline_basis_d(lo + k2, ds.degree, (double)timestamps_[0], ds.knots);
-            }
-            spl_basis_d_.reserve(64 * sizeof(double) * (d + 1));
-            spl_basis_f_.reserve(64 * sizeof(float) * (d + 1));
-            double* bdd = spl_basis_d_.as<double>() + 64 * d;
-            float* bfd = spl_basis_f_.as<float>() + 64 * d;
-            BCSIM_CUDA(cudaMemcpyAsync(bdd, bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-            BCSIM_CUDA(cudaMemcpyAsync(bfd, bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
-            BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
-                                                 spl[d].mu[0] - ds.degree, ds.degree, bdd, bfd, off, origin, p, b,
-                                                 keys_in_.as<uint32_t>(), vals_in_.as<uint32_t>(), recA_.as<float4>(),
-                                                 recB_.as<float4>(), st));
-            BCSIM_CUDA(cudaStreamSynchronize(st));   // bd/bf host vectors are reused
-            spline_off[d] = off;
+            P.spline_off[d] = off;
+            P.spline_first_cs.resize(splines_.size(), 0);
+            P.spline_first_cs[d] = lo;
             off += ds.n;
         }
+        spl_basis_d_.reserve(bd.size() * sizeof(double));
+        spl_basis_f_.reserve(bf.size() * sizeof(float));
+        BCSIM_CUDA(cudaMemcpyAsync(spl_basis_d_.get(), bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        BCSIM_CUDA(cudaMemcpyAsync(spl_basis_f_.get(), bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
         int end_bit = 1;
         while ((1ll << end_bit) < (int64_t)ns + 2) end_bit++;
+        P.end_bit = end_bit;
         size_t tmp_bytes = 0;
         BCSIM_CUDA(radix_sort_pairs(nullptr, &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
                                     vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
         sort_tmp_.reserve(tmp_bytes);
-        BCSIM_CUDA(radix_sort_pairs(sort_tmp_.get(), &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
-                                    vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
-        BCSIM_CUDA(launch_count_keys(keys_out_.as<uint32_t>(), N, ns, counts_.as<int>(), st));
-        BCSIM_CUDA(launch_gather_records(vals_out_.as<uint32_t>(), counts_.as<int>(), N, recA_.as<float4>(),
-                                         recB_.as<float4>(), records_.as<float4>(), N, st));
-        if (store_details_) debug_["prep_sort_ms"].push_back(timer.stop());
-        timer.restart();
-        // records per CTA: enough CTAs to fill the GPU several times over
+        P.sort_tmp_bytes = tmp_bytes;
+        // records per CTA (a multiple of 128 so that results do not depend on it):
+        // enough CTAs to fill the GPU several times over
         int chunk = 1024;
         while (chunk > 128 && (N + chunk - 1) / chunk < 4 * 152) chunk /= 2;
-        if (tile_lines_ > 0) chunk = std::max(64, std::min(4096, tile_lines_));
-        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, chunk, lines_d,
+        P.chunk = chunk;
+        // what the records depend on: scatterers, origin, common time, constants
+        uint64_t key = data_version_ * 1000003ull;
+        auto mix = [&](const void* ptr, size_t n) {
+            const unsigned char* c = static_cast<const unsigned char*>(ptr);
+            for (size_t i = 0; i < n; i++) key = (key ^ c[i]) * 1099511628211ull;
+        };
+        mix(lines_[0].o, sizeof(lines_[0].o));
+        mix(&timestamps_[0], sizeof(float));
+        mix(&p, sizeof(p));
+        mix(&b, sizeof(b));
+        P.records_key = key;
+    }
+    // the host vectors above are pageable: finish their copies before they go
+    BCSIM_CUDA(cudaStreamSynchronize(st));
+    P.version = cfg_version_;
+    if (autotune_) autotune();
+}
+
+// ---------------------------------------------------------------------------
+// enqueue: device work only (capturable: no allocation, no host copy, no sync)
+// ---------------------------------------------------------------------------
+void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
+    const Plan& P = plan_;
+    const SimParams& p = P.p;
+    const BeamDev& b = P.b;
+    const int L = num_lines_;
+    const int ns = (int)ns_;
+    EventTimer total(timing, st);
+    EventTimer timer(timing, st);
+    unsigned long long* bins = bins_.as<unsigned long long>();
+    const LineGeom* lines_d = lines_dev_.as<LineGeom>();
+    BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, st));
+    if (timing) debug_["kernel_memset_ms"].push_back(timer.stop());
+
+    if (P.n_shared > 0) {
+        const int64_t N = P.n_shared;
+        timer.restart();
+        if (!record_cache_ || records_key_ != P.records_key) {
+            const float* origin = lines_[0].o;
+            if (fixed_n_ > 0)
+                BCSIM_CUDA(launch_prep_shared(fixed_xyza_.as<float4>(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
+                                              vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
+            for (size_t d = 0; d < splines_.size(); d++) {
+                if (!P.spline_shared[d]) continue;
+                const SplineDataset& ds = splines_[d];
+                BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                                                     P.spline_first_cs[d], ds.degree, spl_basis_d_.as<double>() + 64 * d,
+                                                     spl_basis_f_.as<float>() + 64 * d, P.spline_off[d], origin, p, b,
+                                                     keys_in_.as<uint32_t>(), vals_in_.as<uint32_t>(),
+                                                     recA_.as<float4>(), recB_.as<float4>(), st));
+            }
+            size_t tmp_bytes = P.sort_tmp_bytes;
+            BCSIM_CUDA(radix_sort_pairs(sort_tmp_.get(), &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
+                                        vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, P.end_bit, st));
+            BCSIM_CUDA(launch_count_keys(keys_out_.as<uint32_t>(), N, ns, counts_.as<int>(), st));
+            BCSIM_CUDA(launch_gather_records(vals_out_.as<uint32_t>(), counts_.as<int>(), N, recA_.as<float4>(),
+                                             recB_.as<float4>(), records_.as<float4>(), N, st));
+            records_key_ = P.records_key;
+        }
+        if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
+        timer.restart();
+        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
                                          line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins, st));
         // near-origin residue, per pair
-        for (const GenLaunch& g : gl) {
+        for (const GenLaunch& g : P.gl) {
             if (g.kind == 0) {
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
                                                   vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
-                                                  gen_line_ids_.as<int>() , gen_tiles_.as<LineTile>() + g.tile_off,
+                                                  gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
                                                   (int)g.num_tiles, nullptr, p, b, bins, st));
-            } else if (spline_shared[g.d]) {
+            } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
                 BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                                   ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
-                                                  spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
+                                                  P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                                   gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
             }
         }
-        if (store_details_) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
+        if (timing) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
     }
 
-    // ---------------- per-pair path ----------------
+    // per-pair path
     timer.restart();
-    for (const GenLaunch& g : gl) {
+    for (const GenLaunch& g : P.gl) {
         if (g.kind == 0) {
-            if (shared) continue;
+            if (P.shared) continue;
             BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
                                               b, bins, st));
         } else {
-            if (spline_shared[g.d]) continue;
+            if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
             BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
@@ -887,24 +936,91 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
                                               gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
         }
     }
-    if (store_details_) debug_[shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
+    if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
 
-    // ---------------- convolution + demodulation + decimation ----------------
+    // convolution + demodulation + decimation
     timer.restart();
-    BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -S), taps_dev_.as<float2>(),
-                                          (int)tap_count_, (int)tap_start_, M_, center_, decimation_, (int)nd_,
-                                          demod_dev_.as<float2>(), dev_out, st));
-    if (store_details_) debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
+    BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -p.log2scale),
+                                          taps_dev_.as<float2>(), (int)tap_count_, (int)tap_start_, M_, center_,
+                                          decimation_, (int)nd_, demod_dev_.as<float2>(), dev_out, st));
+    if (timing) {
+        debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
+        debug_["total_ms"].push_back(total.stop());
+    }
+}
+
+void Simulator::simulate(float2* dev_out, float* host_out) {
+    prepare();
+    if (store_details_) debug_.clear();
+    const cudaStream_t st = stream_;
+    enqueue(st, dev_out, store_details_);
     if (host_out) {
-        timer.restart();
-        BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)L * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
+        EventTimer timer(store_details_, st);
+        BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)num_lines_ * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
         BCSIM_CUDA(cudaStreamSynchronize(st));
         if (store_details_) debug_["kernel_memcpy_ms"].push_back(timer.stop());
-        int flag = 0;
-        BCSIM_CUDA(read_and_clear_error_flag(&flag, st));
-        if (flag) throw SimError(BCSIM_E_INTERNAL, "a bounded device wait gave up; results are incomplete");
+        check_device_flag();
     }
-    if (store_details_) debug_["total_ms"].push_back(total.stop());
+}
+
+void Simulator::check_device_flag() {
+    int flag = 0;
+    BCSIM_CUDA(read_and_clear_error_flag(&flag, stream_));
+    if (flag) throw SimError(BCSIM_E_INTERNAL, "a bounded device wait gave up; results are incomplete");
+}
+
+// Lines-per-tile and records-per-CTA from measurement: every candidate launch
+// shape is timed on this configuration once and the fastest is kept, per shape
+// class (path, beam, phase delay, scatterer and line count buckets).  Tile
+// shapes never change the results (fixed-point sums; FP32 partial sums are
+// aligned to absolute record indices), only the time.
+void Simulator::autotune() {
+    Plan& P = plan_;
+    auto bucket = [](int64_t v) { int b = 0; while (v > 1) { v >>= 1; b++; } return b; };
+    const int64_t n_pairs = total_num_scatterers();
+    const std::string key = std::to_string(P.shared) + "/" + std::to_string(beam_type_) + "/" +
+                            std::to_string(phase_delay_) + "/" + std::to_string(bucket(n_pairs)) + "/" +
+                            std::to_string(bucket(num_lines_)) + "/" + std::to_string(splines_.empty());
+    static std::mutex mtx;
+    static std::map<std::string, std::pair<int, int>> cache;   // key -> (chunk, tile lines)
+    {
+        std::lock_guard<std::mutex> lock(mtx);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+            if (P.n_shared > 0) P.chunk = it->second.first;
+            return;
+        }
+    }
+    std::vector<int> chunks = {P.chunk};
+    if (P.n_shared > 0) chunks = {128, 256, 512, 1024, 2048};
+    const cudaStream_t st = stream_;
+    out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2));
+    cudaEvent_t e0, e1;
+    BCSIM_CUDA(cudaEventCreate(&e0));
+    BCSIM_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_chunk = P.chunk;
+    enqueue(st, out_.as<float2>(), false);   // records, warm-up
+    for (int c : chunks) {
+        P.chunk = c;
+        float ms_min = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+            BCSIM_CUDA(cudaEventRecord(e0, st));
+            enqueue(st, out_.as<float2>(), false);
+            BCSIM_CUDA(cudaEventRecord(e1, st));
+            BCSIM_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            BCSIM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            ms_min = std::min(ms_min, ms);
+        }
+        if (ms_min < best) { best = ms_min; best_chunk = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    P.chunk = best_chunk;
+    std::lock_guard<std::mutex> lock(mtx);
+    cache[key] = {best_chunk, 0};
+    log(0, "autotune " + key + ": records per CTA " + std::to_string(best_chunk));
 }
 
 void Simulator::simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples) {
@@ -927,6 +1043,86 @@ void Simulator::simulate_device(void* dev_out, int64_t cap_complex) {
     if (!dev_out || cap_complex < L * nd)
         throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
     simulate(static_cast<float2*>(dev_out), nullptr);
+}
+
+void Simulator::clone_from(Simulator& o) {
+    o.ensure_device();
+    ensure_device();
+    verbose_ = o.verbose_;
+    sound_speed_ = o.sound_speed_;
+    noise_amplitude_ = o.noise_amplitude_;
+    arc_ = o.arc_;
+    decimation_ = o.decimation_;
+    phase_delay_ = o.phase_delay_;
+    cuda_streams_ = o.cuda_streams_;
+    threads_per_block_ = o.threads_per_block_;
+    mode_ = o.mode_;
+    fir_tail_ = o.fir_tail_;
+    tile_lines_ = o.tile_lines_;
+    cull_ = o.cull_;
+    record_cache_ = o.record_cache_;
+    autotune_ = o.autotune_;
+    excitation_set_ = o.excitation_set_;
+    taps_ = o.taps_;
+    center_ = o.center_;
+    fs_ = o.fs_;
+    fd_ = o.fd_;
+    beam_type_ = o.beam_type_;
+    sigma_l_ = o.sigma_l_;
+    sigma_e_ = o.sigma_e_;
+    lut_ = o.lut_;
+    lut_nr_ = o.lut_nr_; lut_nl_ = o.lut_nl_; lut_ne_ = o.lut_ne_;
+    for (int i = 0; i < 6; i++) lut_ext_[i] = o.lut_ext_[i];
+    lut_absmax_ = o.lut_absmax_;
+    lut_uploaded_ = false;
+    fixed_n_ = o.fixed_n_;
+    num_fixed_sets_ = o.num_fixed_sets_;
+    fixed_sum_abs_ = o.fixed_sum_abs_;
+    amplitude_nonfinite_ = o.amplitude_nonfinite_;
+    if (fixed_n_ > 0) {
+        fixed_xyza_.reserve((size_t)fixed_n_ * sizeof(float4));
+        BCSIM_CUDA(cudaMemcpy(fixed_xyza_.get(), o.fixed_xyza_.get(), (size_t)fixed_n_ * sizeof(float4), cudaMemcpyDeviceToDevice));
+    }
+    splines_.clear();
+    for (const SplineDataset& src : o.splines_) {
+        SplineDataset ds;
+        ds.degree = src.degree;
+        ds.num_cs = src.num_cs;
+        ds.knots = src.knots;
+        ds.n = src.n;
+        ds.sum_abs_amp = src.sum_abs_amp;
+        if (src.n > 0 && src.num_cs > 0) {
+            ds.cps.reserve((size_t)src.num_cs * src.n * sizeof(float4));
+            BCSIM_CUDA(cudaMemcpy(ds.cps.get(), src.cps.get(), (size_t)src.num_cs * src.n * sizeof(float4), cudaMemcpyDeviceToDevice));
+        }
+        if (src.n > 0) {
+            ds.amps.reserve((size_t)src.n * sizeof(float));
+            BCSIM_CUDA(cudaMemcpy(ds.amps.get(), src.amps.get(), (size_t)src.n * sizeof(float), cudaMemcpyDeviceToDevice));
+        }
+        splines_.push_back(std::move(ds));
+    }
+    scan_set_ = false;
+    tables_valid_ = false;
+    lines_valid_ = false;
+    cfg_version_++;
+    data_version_++;
+}
+
+int64_t Simulator::samples_for(float line_length) const { return num_rf_samples(sound_speed_, line_length, fs_); }
+
+size_t Simulator::footprint_bytes(int num_lines, int64_t ns_req) const {
+    size_t n_all = (size_t)fixed_n_;
+    size_t b = (size_t)fixed_n_ * sizeof(float4);
+    for (const auto& d : splines_) {
+        b += (size_t)d.num_cs * d.n * sizeof(float4) + (size_t)d.n * sizeof(float);
+        n_all += d.n;
+    }
+    b += n_all * (4 * sizeof(uint32_t) + 4 * sizeof(float4));        // sort keys/values, records
+    const size_t ns = (size_t)std::max<int64_t>(ns_req, 1);
+    b += (size_t)num_lines * ns * 2 * sizeof(unsigned long long);    // bins
+    b += (size_t)num_lines * ns * sizeof(float2);                    // output (upper bound)
+    b += (size_t)lut_.size() * sizeof(float4);
+    return b;
 }
 
 }  // namespace bcsim_gb300

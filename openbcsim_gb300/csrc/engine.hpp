@@ -59,6 +59,33 @@ struct SplineDataset {
 
 typedef void (*LogFn)(int level, const char* message, void* user);
 
+// One per-pair launch of a simulation: the fixed scatterers (kind 0) or spline
+// dataset d (kind 1), with its line tiles and per-line basis.
+struct GenLaunch {
+    int kind;
+    int d;
+    size_t tile_off, num_tiles, basis_off;
+};
+
+// Host-side plan of one configuration: launch constants and shapes, built by
+// prepare() and reused until the configuration changes.
+struct Plan {
+    uint64_t version = ~0ull;
+    SimParams p;
+    BeamDev b;
+    bool shared = false;
+    int64_t n_shared = 0;
+    std::vector<char> spline_shared;
+    std::vector<int64_t> spline_off;
+    std::vector<int> spline_first_cs;
+    std::vector<GenLaunch> gl;
+    size_t bins_bytes = 0;
+    size_t sort_tmp_bytes = 0;
+    int end_bit = 1;
+    int chunk = 1024;
+    uint64_t records_key = 0;
+};
+
 class Simulator {
 public:
     Simulator();
@@ -83,6 +110,24 @@ public:
     // Runs the pipeline into device memory dev_out (complex64 [L][nd]); if
     // host_out is given, also copies to it and synchronises.
     void simulate(float2* dev_out, float* host_out);
+    // Host work of simulate_lines for the current configuration (cached).
+    void prepare();
+    // Device work of simulate_lines on stream st into dev_out: launches only,
+    // no allocation, no host copy, no synchronisation (can be graph-captured
+    // after prepare()).
+    void enqueue(cudaStream_t st, float2* dev_out, bool timing);
+    // Copy the whole configuration of o (parameters, excitation, beam, scatterer
+    // datasets -- device copies; not the scan sequence) into this simulator.
+    void clone_from(Simulator& o);
+    // Device bytes this simulator holds or will hold for num_lines lines of ns samples.
+    size_t footprint_bytes(int num_lines, int64_t ns) const;
+    // Samples per line this configuration gives for a line length.
+    int64_t samples_for(float line_length) const;
+    int64_t num_lines() const { return num_lines_; }
+    int64_t num_out_samples() const { return nd_; }
+    float2* internal_output() { return out_.as<float2>(); }
+    uint64_t config_version() const { return cfg_version_; }
+    void check_device_flag();
     void simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples);
     void simulate_device(void* dev_out, int64_t cap_complex);
 
@@ -96,6 +141,7 @@ private:
     void throw_if_not_configured() const;
     void prepare_excitation_tables();
     void prepare_lines();
+    void autotune();
     double fixed_point_bound() const;
 
     // configuration
@@ -115,6 +161,12 @@ private:
     double fir_tail_ = 1e-10;
     int tile_lines_ = 0;   // 0 = automatic
     bool cull_ = true;     // exact culling of zero-weight (scatterer, line-slot) pairs
+    bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
+    bool autotune_ = false;
+    uint64_t cfg_version_ = 1;   // bumped by every configuration change
+    uint64_t data_version_ = 1;  // bumped by every scatterer change
+    uint64_t records_key_ = 0;
+    Plan plan_;
 
     bool excitation_set_ = false;
     std::vector<float> taps_;

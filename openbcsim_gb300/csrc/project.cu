@@ -431,7 +431,9 @@ __global__ void __launch_bounds__(256)
         for (int i = 0; i < cnt; i++) {
             const float4 B = smB[i];
             const int idx = __float_as_int(B.w);
-            if (idx != cur || (i & (FOLD - 1)) == FOLD - 1) {
+            // fold at absolute record indices k*FOLD (chunk starts are multiples of
+            // FOLD), so the FP32 partial sums do not depend on the chunk size
+            if (idx != cur || ((start + i) & (FOLD - 1)) == 0) {
 #pragma unroll
                 for (int j = 0; j < LPT; j++) {
                     tr[j] += __float2ll_rn(ar[j] * scale);
