@@ -389,6 +389,130 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "projections/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_batch(args):
+    """Config 4: 64 uneven jobs (fixed and spline, uneven N, L, depth, pulse,
+    decimation).  plain: one simulate_lines per job, in order; batched: one
+    Batch.run (all jobs submitted at once on separate streams, replayed as a
+    CUDA graph).  Both with results on the host."""
+    import torch
+
+    import openbcsim_gb300 as gb
+    from openbcsim_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    jobs = W.batch_uneven(num_jobs=args.jobs, scale=args.batch_scale)
+    sims = []
+    for j in jobs:
+        s = gb.RfSimulator("gpu")
+        gb.configure_job(s, j)
+        apply_params(s, args.param)
+        sims.append(s)
+    outs = [np.empty(s.output_shape(), np.complex64) for s in sims]
+    total = sum(j.projections for j in jobs)
+
+    def plain():
+        for s, o in zip(sims, outs):
+            s.simulate_lines_line_major(o)
+
+    batch = gb.Batch(sims, use_graph=True)
+    for _ in range(args.warmup):
+        plain()
+        batch.run(outs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        plain()
+    t_plain = (time.perf_counter() - t0) / args.steps
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.run(outs)
+    t_batch = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    n_spline = sum(1 for j in jobs if j.splines)
+    return {"metric": METRIC + " (batched uneven jobs)", "value": total / t_batch, "unit": "projections/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"batch_uneven: {len(jobs)} jobs ({n_spline} spline), "
+                                   f"{total:.3e} projections per step, scale {args.batch_scale}",
+                       "l2": "jobs' data far exceed L2"},
+            "plain": {"value": total / t_plain, "ms_per_step": t_plain * 1e3},
+            "batched_over_plain": t_plain / t_batch, "clocks": clk}
+
+
+def run_serve(args):
+    """Config 5: Poisson request stream over 8 resident phantoms, replayed in
+    real time against the continuous-batching server; the same stream run
+    serially (one plain simulate_lines at a time, each starting when the
+    previous one ended or when the request arrived) gives the serial latencies."""
+    import torch
+
+    import openbcsim_gb300 as gb
+    from openbcsim_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    phantoms = W.served_phantoms(scale=args.batch_scale)
+    reqs = W.request_stream(phantoms, rate_hz=args.rate, seconds=args.serve_seconds)
+    sims = []
+    for j in phantoms:
+        s = gb.RfSimulator("gpu")
+        gb.configure_job(s, j)
+        sims.append(s)
+    server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4)
+    pids = [server.add_phantom(s) for s in sims]
+    # warm-up: one request per phantom
+    for k, s in enumerate(phantoms):
+        sc = s.scan
+        server.wait(server.submit(pids[k], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
+                                  sc.timestamps, 8))
+    ids = []
+    t_start = time.perf_counter()
+    for r in reqs:
+        now = time.perf_counter() - t_start
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
+        sc = r.scan
+        ids.append(server.submit(pids[r.phantom], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
+                                 sc.timestamps, r.decimation))
+    lat = [server.wait(i)[1] for i in ids]
+    wall = time.perf_counter() - t_start
+    st = server.stats()
+    server.close()
+    n_proj = sum(phantoms[r.phantom].num_scatterers * r.scan.num_lines for r in reqs)
+    # serial plain execution of the same stream
+    service = []
+    for r in reqs:
+        s = sims[r.phantom]
+        sc = r.scan
+        t0 = time.perf_counter()
+        s.set_parameter("radial_decimation", str(r.decimation))
+        s.set_scan_sequence(sc.origins, sc.directions, sc.line_length, sc.lateral_dirs, sc.timestamps)
+        s.simulate_lines_line_major()
+        service.append(time.perf_counter() - t0)
+    finish, serial_lat = 0.0, []
+    for r, sv in zip(reqs, service):
+        start = max(r.arrival, finish)
+        finish = start + sv
+        serial_lat.append((finish - r.arrival) * 1e3)
+    lat_sorted, ser_sorted = sorted(lat), sorted(serial_lat)
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+
+    return {"metric": METRIC + " (served stream)", "value": n_proj / wall, "unit": "projections/s",
+            "n_gpus": 1, "steps": len(reqs), "warmup": len(phantoms), "ms_per_step": wall * 1e3 / max(1, len(reqs)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": f"served_stream: {len(reqs)} requests, Poisson {args.rate}/s over "
+                                   f"{args.serve_seconds} s, 8 resident phantoms (scale {args.batch_scale})"},
+            "latency_ms": {"p50": pct(lat_sorted, 0.5), "p99": pct(lat_sorted, 0.99), "max": lat_sorted[-1]},
+            "serial_plain": {"latency_ms": {"p50": pct(ser_sorted, 0.5), "p99": pct(ser_sorted, 0.99)},
+                             "busy_s": sum(service), "value": n_proj / sum(service)},
+            "server_stats": st}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,6 +526,12 @@ def main():
     ap.add_argument("--num-scatterers", type=int, default=0, help="override the workload's scatterer count")
     ap.add_argument("--lines", default="", help="override the line count (volume: 'n_az,n_el')")
     ap.add_argument("--param", action="append", default=[], help="engine parameter key=value (repeatable)")
+    ap.add_argument("--mode", default="single", choices=["single", "batch", "serve"],
+                    help="single: the headline workload; batch: 64 uneven jobs; serve: Poisson request stream")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of N and L in batch/serve modes")
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--simulate-only", action="store_true", help="only run warmup+steps simulations (profiling)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per projection launch from an ncu capture (reported as roofline.traffic)")
@@ -411,7 +541,12 @@ def main():
         return
     if args.warmup < 3:
         args.warmup = 3
-    res = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if args.mode == "batch":
+        res = run_batch(args)
+    elif args.mode == "serve":
+        res = run_serve(args)
+    else:
+        res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:
         print(json.dumps(res), flush=True)
 

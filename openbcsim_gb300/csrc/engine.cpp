@@ -427,22 +427,30 @@ void Simulator::prepare_excitation_tables() {
     nd_ = (ns_ + decimation_ - 1) / decimation_;
     if (center_ < 0 || (int64_t)center_ + (nd_ - 1) * decimation_ >= M_)
         throw SimError(BCSIM_E_INVALID, "excitation center index outside the convolution buffer");
-    const auto ha = analytic_pulse(taps_, M_);
-    choose_tap_window(ha, (int)ntaps, fir_tail_, &tap_start_, &tap_count_);
-    std::vector<float2> taps((size_t)tap_count_);
-    for (int64_t w = 0; w < tap_count_; w++) {
-        const int64_t n = ((tap_start_ + w) % M_ + M_) % M_;
-        taps[w] = make_float2((float)ha[n].real(), (float)ha[n].imag());
+    // the FIR window depends on the excitation, M and the tail energy only:
+    // recompute it (an M-point FFT in double) only when one of them changed
+    if (!(fir_key_taps_ == taps_ && fir_key_M_ == M_ && fir_key_tail_ == fir_tail_)) {
+        const auto ha = analytic_pulse(taps_, M_);
+        choose_tap_window(ha, (int)ntaps, fir_tail_, &tap_start_, &tap_count_);
+        std::vector<float2> taps((size_t)tap_count_);
+        for (int64_t w = 0; w < tap_count_; w++) {
+            const int64_t n = ((tap_start_ + w) % M_ + M_) % M_;
+            taps[w] = make_float2((float)ha[n].real(), (float)ha[n].imag());
+        }
+        taps_dev_.reserve(taps.size() * sizeof(float2));
+        BCSIM_CUDA(cudaMemcpyAsync(taps_dev_.get(), taps.data(), taps.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
+        BCSIM_CUDA(cudaStreamSynchronize(stream_));
+        fir_key_taps_ = taps_;
+        fir_key_M_ = M_;
+        fir_key_tail_ = fir_tail_;
+        log(0, "FIR window: start " + std::to_string(tap_start_) + ", taps " + std::to_string(tap_count_) + ", M " +
+                   std::to_string(M_));
     }
-    taps_dev_.reserve(taps.size() * sizeof(float2));
-    BCSIM_CUDA(cudaMemcpyAsync(taps_dev_.get(), taps.data(), taps.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     const auto dm = demod_factors(fd_, fs_, decimation_, nd_, mode_ == MODE_REFERENCE);
     demod_dev_.reserve(dm.size() * sizeof(float2));
     BCSIM_CUDA(cudaMemcpyAsync(demod_dev_.get(), dm.data(), dm.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
     tables_valid_ = true;
-    log(0, "FIR window: start " + std::to_string(tap_start_) + ", taps " + std::to_string(tap_count_) + ", M " +
-               std::to_string(M_));
 }
 
 // Kernel line order for the shared-origin kernel: lines sorted along a Morton
@@ -486,30 +494,31 @@ static void order_lines(const std::vector<LineGeom>& lines, std::vector<int>& or
     }
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
     const int slots = (L + 31) / 32;
-    cones.assign(slots, SlotCone{0, 0, 1, -1, 0, 0, 0, 0});
+    cones.assign(slots, SlotCone{0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2});
     for (int s = 0; s < slots; s++) {
-        double c[3] = {0, 0, 0};
         const int lo = s * 32, hi = std::min(L, lo + 32);
-        for (int i = lo; i < hi; i++)
-            for (int k = 0; k < 3; k++) c[k] += lines[order[i]].d[k];
-        const double cn = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
-        double alpha = M_PI;
-        if (cn > 1e-9) {
-            for (double& x : c) x /= cn;
-            alpha = 0.0;
-            for (int i = lo; i < hi; i++) {
-                const float* d = lines[order[i]].d;
-                const double dn = std::sqrt((double)d[0] * d[0] + (double)d[1] * d[1] + (double)d[2] * d[2]);
-                const double cosang = std::max(-1.0, std::min(1.0, (d[0] * c[0] + d[1] * c[1] + d[2] * c[2]) / dn));
-                alpha = std::max(alpha, std::acos(cosang));
+        const LineGeom& ref = lines[order[(lo + hi) / 2]];
+        double du = 0, dv = 0, dd = 0;
+        for (int i = lo; i < hi; i++) {
+            const LineGeom& g = lines[order[i]];
+            double a = 0, b = 0, c = 0;
+            for (int k = 0; k < 3; k++) {
+                a += ((double)g.l[k] - ref.l[k]) * ((double)g.l[k] - ref.l[k]);
+                b += ((double)g.e[k] - ref.e[k]) * ((double)g.e[k] - ref.e[k]);
+                c += ((double)g.d[k] - ref.d[k]) * ((double)g.d[k] - ref.d[k]);
             }
-            alpha += 1e-4;   // margin for float rounding of the axis and the test
+            du = std::max(du, std::sqrt(a));
+            dv = std::max(dv, std::sqrt(b));
+            dd = std::max(dd, std::sqrt(c));
         }
         SlotCone cone;
-        cone.cx = (float)c[0]; cone.cy = (float)c[1]; cone.cz = (float)c[2];
-        cone.cos_a = alpha >= M_PI / 2 ? -1.0f : (float)std::cos(alpha);
-        cone.sin_a = alpha >= M_PI / 2 ? 1.0f : (float)std::sin(alpha);
-        cone.pad0 = cone.pad1 = cone.pad2 = 0.0f;
+        cone.lx = ref.l[0]; cone.ly = ref.l[1]; cone.lz = ref.l[2];
+        cone.ex = ref.e[0]; cone.ey = ref.e[1]; cone.ez = ref.e[2];
+        cone.rx = ref.d[0]; cone.ry = ref.d[1]; cone.rz = ref.d[2];
+        // margin for the float rounding of the test's dot products
+        cone.du = (float)(du * 1.0001 + 2e-6);
+        cone.dv = (float)(dv * 1.0001 + 2e-6);
+        cone.dd = (float)(dd * 1.0001 + 2e-6);
         cones[s] = cone;
     }
 }
@@ -664,22 +673,24 @@ void Simulator::prepare() {
     S = std::max(-100, std::min(100, S));
     p.log2scale = S;
     p.scale = std::ldexp(1.0f, S);
-    // exact culling radius (fp64 mode): beyond it the weight is exactly 0
+    // exact culling ranges (fp64 mode): outside them the weight is exactly 0
     if (mode_ == MODE_FP64 && cull_) {
-        double r = 0.0;
+        double llo, lhi, elo, ehi;
         if (beam_type_ == BEAM_GAUSSIAN) {
-            // exp2f(-q) is exactly 0 for q >= 151, q = l^2 gl + e^2 ge >= dist^2 min(gl, ge)
-            r = std::sqrt(151.0 / std::min((double)b.gl, (double)b.ge));
+            // exp2f(-q) is exactly 0 for q >= 151, q = l^2 gl + e^2 ge
+            const double rl = std::sqrt(151.0 / (double)b.gl), re = std::sqrt(151.0 / (double)b.ge);
+            llo = -rl; lhi = rl; elo = -re; ehi = re;
         } else {
             // table coordinate -1 < t < n-1  <=>  first - spacing < x < last
-            const double rl = std::max(std::fabs((double)lut_ext_[2] - b.dl), std::fabs((double)lut_ext_[3]));
-            const double re = std::max(std::fabs((double)lut_ext_[4] - b.de), std::fabs((double)lut_ext_[5]));
-            r = std::sqrt(rl * rl + re * re);
+            llo = (double)lut_ext_[2] - b.dl; lhi = lut_ext_[3];
+            elo = (double)lut_ext_[4] - b.de; ehi = lut_ext_[5];
         }
-        r = r * 1.001 + 1e-7;
-        p.cull = std::isfinite(r) ? 1 : 0;
-        p.cull_r = (float)r;
-        p.cull_r2 = (float)(r * r);
+        const double ml = 1e-3 * (std::fabs(llo) + std::fabs(lhi)) + 1e-7;
+        const double me = 1e-3 * (std::fabs(elo) + std::fabs(ehi)) + 1e-7;
+        p.cull = std::isfinite(llo + lhi + elo + ehi) ? 1 : 0;
+        p.cull_l_lo = (float)(llo - ml); p.cull_l_hi = (float)(lhi + ml);
+        p.cull_e_lo = (float)(elo - me); p.cull_e_hi = (float)(ehi + me);
+        p.cull_rho_per_bin = (float)((double)sound_speed_ / (2.0 * (double)fs_) * 1.0001);
     }
 
     // per-line spline knot intervals and basis (CpuAlgorithm.cpp:101-133)
@@ -992,7 +1003,7 @@ void Simulator::autotune() {
         }
     }
     std::vector<int> chunks = {P.chunk};
-    if (P.n_shared > 0) chunks = {128, 256, 512, 1024, 2048};
+    if (P.n_shared > 0) chunks = {128, 256, 512, 1024};
     const cudaStream_t st = stream_;
     out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2));
     cudaEvent_t e0, e1;

@@ -203,6 +203,9 @@ private:
     bool tables_valid_ = false;
     int64_t M_ = 0, nd_ = 0;
     int64_t tap_start_ = 0, tap_count_ = 0;
+    std::vector<float> fir_key_taps_;   // inputs of the current FIR window
+    int64_t fir_key_M_ = -1;
+    double fir_key_tail_ = -1.0;
     DeviceBuffer taps_dev_, demod_dev_;
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;

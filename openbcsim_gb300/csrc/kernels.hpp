@@ -47,16 +47,20 @@ struct SimParams {
     float two_pi_fd_over_fs;   // phase per sample of sub-sample delay
     float scale;               // fixed-point scale 2^S for bin accumulation
     int log2scale;
-    // exact culling in the shared-origin kernel: a scatterer farther than
-    // cull_radius from a line's axis has weight exactly 0 on that line
+    // exact culling in the shared-origin kernel: a line's weight is exactly 0
+    // outside cull_l_lo < l < cull_l_hi, cull_e_lo < e < cull_e_hi
     int cull;
-    float cull_r2, cull_r;
+    float cull_l_lo, cull_l_hi, cull_e_lo, cull_e_hi;
+    float cull_rho_per_bin;    // upper bound of 1 / (2 fs / c)
 };
 
-// Bounding cone of a slot of 32 lines (consecutive in the kernel's line order):
-// every line direction is within angle alpha of the unit axis c.
+// Frame spread of a slot of 32 lines (consecutive in the kernel's line order):
+// a reference frame (lateral l, elevational e, radial r) and the largest
+// difference between any line's frame vector and it (du, dv, dd), so that for a
+// scatterer at distance rho every line's coordinate lies within rho * d of the
+// reference coordinate.
 struct SlotCone {
-    float cx, cy, cz, cos_a, sin_a, pad0, pad1, pad2;
+    float lx, ly, lz, ex, ey, ez, rx, ry, rz, du, dv, dd;
 };
 
 // A tile of lines for the per-pair projection kernel: `count` lines taken from

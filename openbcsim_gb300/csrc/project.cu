@@ -322,8 +322,6 @@ __device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
 // Records per folding of the FP32 run sum into the integer bin total: bounds
 // the length of any FP32 summation to FOLD terms.
 constexpr int FOLD = 128;
-// Lines per thread in the shared-origin kernel.
-constexpr int LPT = 2;
 
 // Per-line constants of the shared-origin kernel (fp64 mode):
 //   Gaussian: u = lateral * sqrt(gl), v = elevational * sqrt(ge), so that the
@@ -355,16 +353,25 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
     return k;
 }
 
-// One CTA: a chunk of `chunk` consecutive records (sorted by bin) staged once in
-// shared memory by a TMA bulk copy, then for every group of blockDim * LPT
-// lines, each thread walks all records for its LPT lines.  Records are
-// broadcast from shared memory and the bin-change branch is warp-uniform; a
-// line's contributions to one bin are summed in FP32, folded into an int64
-// total every FOLD records, and written when the bin changes -- a plain store
-// for bins strictly inside the chunk (no other CTA holds records there), an
-// integer atomic for the chunk's first and last bin.
+// One CTA: a chunk of `chunk` (<= 1024) consecutive records, sorted by bin,
+// staged once in shared memory by a TMA bulk copy; then, for every group of
+// blockDim lines (one per thread, in direction order so that a warp's 32 lines
+// point in nearby directions), two phases per warp:
+//   A. mask: each lane tests one record against the warp's "slot box": the
+//      lateral/elevational ranges outside which every line of the slot has
+//      weight exactly 0 (the lookup table's extent, or where exp2 underflows),
+//      widened by the spread of the slot's line frames times the record's
+//      distance bound.  32 records per instruction; one ballot word per 32
+//      records, word w kept by lane w.
+//   B. walk: only the records whose bit is set, in bin order.  A line's
+//      contributions to one bin are summed in FP32, folded into an int64 total
+//      at absolute record indices k*FOLD, and written when the bin changes: a
+//      plain store for bins strictly inside the chunk (no other CTA holds
+//      records there), an integer atomic for the chunk's first and last bin.
+// Skipped records contribute exactly 0, so the result is bit-identical to
+// walking every record (cull=off), and does not depend on the chunk size.
 template <bool PD, int BEAM, bool REF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     project_shared_kernel(const float4* __restrict__ records, int64_t plane, const int* __restrict__ counts, int chunk,
                           const LineGeom* __restrict__ lines, const int* __restrict__ line_order,
                           const SlotCone* __restrict__ cones, int L, unsigned long long* __restrict__ bins,
@@ -376,6 +383,7 @@ __global__ void __launch_bounds__(256)
     if (start >= n_valid) return;
     const int cnt = (int)min((int64_t)chunk, (int64_t)n_valid - start);
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     float4* smA = sm;
     float4* smB = sm + chunk;
 
@@ -403,104 +411,111 @@ __global__ void __launch_bounds__(256)
     // lookup-table coordinate ranges -1 < t < n-1 as |t - c| < h
     const float cl = 0.5f * (float)(b.nl - 2), hl = 0.5f * (float)b.nl;
     const float ce = 0.5f * (float)(b.ne - 2), he = 0.5f * (float)b.ne;
-
     const bool cull = !REF && p.cull;
-    for (int g0 = 0; g0 < L; g0 += blockDim.x * LPT) {
-        LineK k[LPT];
-        bool active[LPT];
-        unsigned long long* lb[LPT];
-        float ccx[LPT], ccy[LPT], ccz[LPT], cca[LPT], csa[LPT];
-#pragma unroll
-        for (int j = 0; j < LPT; j++) {
-            const int slot_pos = g0 + j * blockDim.x + tid;
-            active[j] = slot_pos < L;
-            const int line = __ldg(line_order + (active[j] ? slot_pos : L - 1));
-            k[j] = load_line<BEAM, REF>(lines + line, b);
-            lb[j] = bins + (int64_t)line * p.ns * stride;
-            // cone of this warp's 32 lines (slot_pos / 32 is uniform in the warp)
-            const SlotCone* c = cones + min(slot_pos, L - 1) / 32;
-            ccx[j] = __ldg(&c->cx); ccy[j] = __ldg(&c->cy); ccz[j] = __ldg(&c->cz);
-            cca[j] = __ldg(&c->cos_a); csa[j] = __ldg(&c->sin_a) * p.cull_r;
-        }
-        int cur = first_bin;
-        long long tr[LPT], ti[LPT];
-        float ar[LPT], ai[LPT];
-#pragma unroll
-        for (int j = 0; j < LPT; j++) { tr[j] = 0; ti[j] = 0; ar[j] = 0.0f; ai[j] = 0.0f; }
+    const int nwords = (cnt + 31) >> 5;
 
-        for (int i = 0; i < cnt; i++) {
-            const float4 B = smB[i];
-            const int idx = __float_as_int(B.w);
-            // fold at absolute record indices k*FOLD (chunk starts are multiples of
-            // FOLD), so the FP32 partial sums do not depend on the chunk size
-            if (idx != cur || ((start + i) & (FOLD - 1)) == 0) {
-#pragma unroll
-                for (int j = 0; j < LPT; j++) {
-                    tr[j] += __float2ll_rn(ar[j] * scale);
-                    if (PD) ti[j] += __float2ll_rn(ai[j] * scale);
-                    ar[j] = 0.0f;
-                    ai[j] = 0.0f;
+    for (int g0 = 0; g0 < L; g0 += blockDim.x) {
+        const int slot_pos = g0 + tid;
+        const bool active = slot_pos < L;
+        const int line = __ldg(line_order + (active ? slot_pos : L - 1));
+        const LineK q = load_line<BEAM, REF>(lines + line, b);
+        unsigned long long* lb = bins + (int64_t)line * p.ns * stride;
+
+        // ---- phase A: records this warp's lines can see ----
+        unsigned mask = 0xffffffffu;
+        if (cull) {
+            const SlotCone* c = cones + min(g0 + (tid & ~31), L - 1) / 32;   // warp-uniform
+            const float lx = __ldg(&c->lx), ly = __ldg(&c->ly), lz = __ldg(&c->lz);
+            const float ex = __ldg(&c->ex), ey = __ldg(&c->ey), ez = __ldg(&c->ez);
+            const float rx = __ldg(&c->rx), ry = __ldg(&c->ry), rz = __ldg(&c->rz);
+            const float du = __ldg(&c->du), dv = __ldg(&c->dv), dd = __ldg(&c->dd);
+            mask = 0;
+            for (int w = 0; w < nwords; w++) {
+                const int r = (w << 5) + lane;
+                bool pass = false;
+                if (r < cnt) {
+                    const float4 A = smA[r];
+                    const int idx = __float_as_int(smB[r].w);
+                    // distance bound from the bin: rho*k <= idx + 1/2
+                    const float rho = ((float)idx + 0.5f) * p.cull_rho_per_bin;
+                    const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
+                    const float v = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
+                    const float dt = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
+                    const float su = rho * du, sv = rho * dv;
+                    pass = (u + su > p.cull_l_lo) && (u - su < p.cull_l_hi) && (v + sv > p.cull_e_lo) &&
+                           (v - sv < p.cull_e_hi) && (dt + rho * dd >= 0.0f);
                 }
-                if (idx != cur) {
-                    const bool edge = cur == first_bin || cur == last_bin;
-#pragma unroll
-                    for (int j = 0; j < LPT; j++) {
-                        if (active[j]) {
-                            unsigned long long* dst = lb[j] + (int64_t)cur * stride;
-                            if (edge) {
-                                if (tr[j]) atomicAdd(dst, (unsigned long long)tr[j]);
-                                if (PD && ti[j]) atomicAdd(dst + 1, (unsigned long long)ti[j]);
+                const unsigned m = __ballot_sync(0xffffffffu, pass);
+                if (lane == w) mask = m;
+            }
+        }
+
+        // ---- phase B: walk the selected records in bin order ----
+        int cur = first_bin;
+        long long tr = 0, ti = 0;
+        float ar = 0.0f, ai = 0.0f;
+        int64_t fold_block = start / FOLD;
+        for (int w = 0; w < nwords; w++) {
+            unsigned word = cull ? __shfl_sync(0xffffffffu, mask, w) : 0xffffffffu;
+            if (!cull && w == nwords - 1 && (cnt & 31)) word &= (1u << (cnt & 31)) - 1u;
+            while (word) {
+                const int i = (w << 5) + __ffs(word) - 1;
+                word &= word - 1u;
+                const float4 B = smB[i];
+                const int idx = __float_as_int(B.w);
+                const int64_t blk = (start + i) / FOLD;
+                // fold at absolute record indices k*FOLD (chunk starts are multiples
+                // of FOLD), so the FP32 partial sums do not depend on the chunk size
+                if (idx != cur || blk != fold_block) {
+                    tr += __float2ll_rn(ar * scale);
+                    if (PD) ti += __float2ll_rn(ai * scale);
+                    ar = 0.0f;
+                    ai = 0.0f;
+                    fold_block = blk;
+                    if (idx != cur) {
+                        if (active) {
+                            unsigned long long* dst = lb + (int64_t)cur * stride;
+                            if (cur == first_bin || cur == last_bin) {
+                                if (tr) atomicAdd(dst, (unsigned long long)tr);
+                                if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
                             } else {
-                                if (tr[j]) dst[0] = (unsigned long long)tr[j];
-                                if (PD && ti[j]) dst[1] = (unsigned long long)ti[j];
+                                if (tr) dst[0] = (unsigned long long)tr;
+                                if (PD && ti) dst[1] = (unsigned long long)ti;
                             }
                         }
-                        tr[j] = 0;
-                        ti[j] = 0;
+                        tr = 0;
+                        ti = 0;
+                        cur = idx;
                     }
-                    cur = idx;
                 }
-            }
-            const float4 A = smA[i];
-            // the scatterer sits farther than cull_r from every axis of a slot when
-            // its angle to the slot axis exceeds alpha + asin(cull_r / rho):
-            // cos(angle) < (sqrt(rho^2 - r^2) cos(alpha) - r sin(alpha)) / rho
-            float sfar = 0.0f;
-            if (cull) sfar = sqrtf(fmaxf(fmaf(A.z, A.z, fmaf(A.y, A.y, A.x * A.x)) - p.cull_r2, 0.0f));
-#pragma unroll
-            for (int j = 0; j < LPT; j++) {
-                const LineK& q = k[j];
-                if (cull) {
-                    const float dc = fmaf(A.z, ccz[j], fmaf(A.y, ccy[j], A.x * ccx[j]));
-                    if (dc < fmaf(sfar, cca[j], -csa[j])) continue;   // warp-uniform
-                }
-                float w;
+                const float4 A = smA[i];
+                float w8;
                 if (REF) {
                     // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
                     const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
                     const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
                     const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
                     if (BEAM == BEAM_GAUSSIAN) {
-                        w = gauss_weight_ref(b, l, e);
+                        w8 = gauss_weight_ref(b, l, e);
                     } else {
                         // the reference recomputes the radial table coordinate per pair from r
-                        w = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
-                                                                  __fmul_rn(A.z, A.z))),
-                                           l, e);
+                        w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                                   __fmul_rn(A.z, A.z))),
+                                            l, e);
                     }
-                    w = signbit(dot) ? 0.0f : w;
+                    w8 = signbit(dot) ? 0.0f : w8;
                 } else {
                     const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
                     const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
                     const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
                     if (BEAM == BEAM_GAUSSIAN) {
-                        w = exp2f(-fmaf(u, u, v * v));
+                        w8 = exp2f(-fmaf(u, u, v * v));
                         // arc projection: a line for which the scatterer lies behind the
                         // origin sees it at -rho, outside [0, ns) for every record
                         // (near-origin scatterers take the per-pair path)
-                        w = signbit(dot) ? 0.0f : w;
+                        w8 = signbit(dot) ? 0.0f : w8;
                     } else {
-                        w = 0.0f;
+                        w8 = 0.0f;
                         if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
                             const int l0 = (int)u, e0 = (int)v;
                             const float fl = u < 0.0f ? 0.0f : u - (float)l0;
@@ -516,36 +531,29 @@ __global__ void __launch_bounds__(256)
                             const float c11 = fmaf(fr, Q.w - Q.y, Q.y);
                             const float c0 = fmaf(fl, c10 - c00, c00);
                             const float c1 = fmaf(fl, c11 - c01, c01);
-                            w = fmaf(fe, c1 - c0, c0);
+                            w8 = fmaf(fe, c1 - c0, c0);
                         }
                     }
                 }
-                ar[j] = fmaf(w, A.w, ar[j]);
-                if (PD) ai[j] = fmaf(w, B.x, ai[j]);
+                ar = fmaf(w8, A.w, ar);
+                if (PD) ai = fmaf(w8, B.x, ai);
             }
         }
-        const bool edge = cur == first_bin || cur == last_bin;
-#pragma unroll
-        for (int j = 0; j < LPT; j++) {
-            tr[j] += __float2ll_rn(ar[j] * scale);
-            if (PD) ti[j] += __float2ll_rn(ai[j] * scale);
-            if (active[j]) {
-                unsigned long long* dst = lb[j] + (int64_t)cur * stride;
-                if (edge) {
-                    if (tr[j]) atomicAdd(dst, (unsigned long long)tr[j]);
-                    if (PD && ti[j]) atomicAdd(dst + 1, (unsigned long long)ti[j]);
-                } else {
-                    if (tr[j]) dst[0] = (unsigned long long)tr[j];
-                    if (PD && ti[j]) dst[1] = (unsigned long long)ti[j];
-                }
+        tr += __float2ll_rn(ar * scale);
+        if (PD) ti += __float2ll_rn(ai * scale);
+        if (active) {
+            unsigned long long* dst = lb + (int64_t)cur * stride;
+            if (cur == first_bin || cur == last_bin) {
+                if (tr) atomicAdd(dst, (unsigned long long)tr);
+                if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
+            } else {
+                if (tr) dst[0] = (unsigned long long)tr;
+                if (PD && ti) dst[1] = (unsigned long long)ti;
             }
         }
     }
 }
 
-// ---------------------------------------------------------------------------
-// per-pair projection
-// ---------------------------------------------------------------------------
 // Scatterers per staged chunk of the per-pair kernel (lines per CTA:
 // PAIR_THREADS in kernels.hpp).
 constexpr int PAIR_CHUNK = 256;
@@ -856,13 +864,13 @@ static cudaError_t launch_shared_t(const float4* records, int64_t plane, const i
                                    const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
                                    const SimParams& p, const BeamDev& b, unsigned long long* bins,
                                    cudaStream_t stream) {
+    if (chunk > 1024 || chunk % FOLD) return cudaErrorInvalidValue;
     const size_t smem = 2 * (size_t)chunk * sizeof(float4);
+    const int64_t chunks = (n + chunk - 1) / chunk;
     auto k = project_shared_kernel<PD, BEAM, REF>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int per = (L + LPT - 1) / LPT;
-    const int threads = per >= 256 ? 256 : ((per + 31) / 32) * 32;
-    const int64_t chunks = (n + chunk - 1) / chunk;
+    const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
     k<<<(unsigned)chunks, threads, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
                                                    p, b);
     return cudaGetLastError();

@@ -340,3 +340,57 @@ def batch_uneven(num_jobs=64, seed=4000, scale=1.0) -> List[Job]:
             scan = sector_scan(L, 35.0, depth, timestamps=ts)
             jobs.append(_excitation_job(f"job{j}_spline", scan, fc, bw, GaussianBeam(1e-3, 1e-3), [], [sp], dec))
     return jobs
+
+
+# ---------------------------------------------------------------------------
+# served request stream
+# ---------------------------------------------------------------------------
+def served_phantoms(seed=5000, scale=1.0) -> List[Job]:
+    """Eight resident phantoms: fixed 100k, 500k, 1M, 2M scatterers and spline
+    50k, 100k, 250k, 500k scatterers with 8, 12, 16, 24 control points; Gaussian
+    beam 1 mm, 2.5 MHz / bw 0.1 / 50 MHz, 12 cm lines.  The scan lines of a job
+    are placeholders: every request brings its own."""
+    out = []
+    for i, n in enumerate([100_000, 500_000, 1_000_000, 2_000_000]):
+        rng = np.random.default_rng(seed + i)
+        fixed = random_fixed(rng, max(16, int(n * scale)), (-0.03, 0.03), None, (0.01, 0.12))
+        out.append(_excitation_job(f"fixed{n}", sector_scan(2, 35.0, 0.12), 2.5e6, 0.1,
+                                   GaussianBeam(1e-3, 1e-3), [fixed], [], 8))
+    for i, (n, K) in enumerate([(50_000, 8), (100_000, 12), (250_000, 16), (500_000, 24)]):
+        rng = np.random.default_rng(seed + 10 + i)
+        sp = random_spline(rng, max(16, int(n * scale)), K)
+        out.append(_excitation_job(f"spline{n}", sector_scan(2, 35.0, 0.12, timestamps=[0.0, 0.5]), 2.5e6, 0.1,
+                                   GaussianBeam(1e-3, 1e-3), [], [sp], 8))
+    return out
+
+
+@dataclass
+class Request:
+    arrival: float          # seconds from the start of the stream
+    phantom: int
+    scan: ScanSequence
+    decimation: int
+
+
+def request_stream(phantoms: List[Job], rate_hz=200.0, seconds=60.0, seed=5100, max_lines=256) -> List[Request]:
+    """Poisson arrivals at rate_hz; each request: 1..max_lines lines at random
+    angles in +-35 degrees and random timestamps in the phantom's time range,
+    decimation 4..16."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate_hz)
+        if t >= seconds:
+            break
+        k = int(rng.integers(0, len(phantoms)))
+        L = int(rng.integers(1, max_lines + 1))
+        job = phantoms[k]
+        if job.splines:
+            sp = job.splines[0]
+            t0, t1 = spline_time_limits(sp.degree, sp.knots, sp.control_points.shape[1])
+            ts = rng.uniform(t0, t1, L)
+        else:
+            ts = rng.uniform(0.0, 1.0, L)
+        scan = sector_scan(L, 35.0, 0.12, timestamps=ts.astype(np.float32), angles_deg=rng.uniform(-35.0, 35.0, L))
+        out.append(Request(t, k, scan, int(rng.integers(4, 17))))
+    return out
