@@ -12,90 +12,169 @@
 // that holds all but a stated fraction of its energy (chosen on the host), then
 // applies the demodulation factor of output m.
 //
-// Layout: one CTA per (line, block of OUT_PER_CTA outputs).  The bins the block
+// Layout: one CTA per (line, block of THREADS*4 outputs).  The bins the block
 // needs are converted from fixed point and staged in shared memory split into D
-// polyphase rows, so that for every tap the threads of a warp read consecutive
-// words (tap w of output m reads row (W-1-w) mod D, column m + (W-1-w) div D).
+// polyphase rows: with q = (m - m0) * D + (W - 1 - w) the segment index of tap w
+// of output m, row q mod D holds the elements of one phase, so that a phase's
+// taps walk along one row.  Each thread computes 4 consecutive outputs; along a
+// row they need consecutive elements, held in a rotating window of 4 registers:
+// one shared-memory load and one (broadcast) tap load per 16 complex MACs.  The
+// taps are stored phase-major on the host, zero-padded to a multiple of 4 per
+// phase.
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "kernels.hpp"
 
 namespace bcsim_gb300 {
 
-constexpr int OUT_PER_CTA = 256;
+constexpr int CONV_K = 4;   // outputs per thread
 
-template <bool PD>
-__global__ void __launch_bounds__(OUT_PER_CTA)
-    convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
-                               const float2* __restrict__ taps, int W, int tap_start, int64_t M, int center, int D,
-                               int nd, const float2* __restrict__ demod, float2* __restrict__ out) {
-    extern __shared__ float2 seg[];
-    const int line = blockIdx.y;
-    const int m0 = blockIdx.x * OUT_PER_CTA;
-    const int tid = threadIdx.x;
-    // bins index of segment element q:  j = jbase + q
-    const int64_t k0 = (int64_t)center + (int64_t)m0 * D;
-    const int64_t jbase = k0 - tap_start - (W - 1);
-    const int seg_len = (OUT_PER_CTA - 1) * D + W;
-    const int row = (seg_len + D - 1) / D;   // polyphase row length
-    const int stride = PD ? 2 : 1;
-    const long long* lb = (const long long*)bins + (int64_t)line * ns * stride;
-    for (int q = tid; q < seg_len; q += OUT_PER_CTA) {
-        int64_t j = (jbase + q) % M;
-        if (j < 0) j += M;
-        float2 v = make_float2(0.0f, 0.0f);
-        if (j < ns) {
-            v.x = __ll2float_rn(__ldg(lb + j * stride)) * inv_scale;
-            if (PD) v.y = __ll2float_rn(__ldg(lb + j * stride + 1)) * inv_scale;
-        }
-        seg[(q % D) * row + q / D] = v;
-    }
-    __syncthreads();
-    const int m = m0 + tid;
-    if (m >= nd) return;
-    float yr = 0.0f, yi = 0.0f;
-    // output m uses segment elements q = (m - m0) * D + (W - 1 - w), w = 0 .. W-1
-    int ph = (W - 1) % D, col = tid + (W - 1) / D;
-    for (int w = 0; w < W; w++) {
-        const float2 h = __ldg(taps + w);
-        const float2 v = seg[ph * row + col];
-        if (PD) {
-            yr = fmaf(v.x, h.x, fmaf(-v.y, h.y, yr));
-            yi = fmaf(v.x, h.y, fmaf(v.y, h.x, yi));
-        } else {
-            yr = fmaf(v.x, h.x, yr);
-            yi = fmaf(v.x, h.y, yi);
-        }
-        // next tap: q decreases by one
-        if (ph == 0) { ph = D - 1; col -= 1; } else { ph -= 1; }
-    }
-    const float2 dm = __ldg(demod + m);
-    out[(int64_t)line * nd + m] = make_float2(yr * dm.x - yi * dm.y, yr * dm.y + yi * dm.x);
+__device__ __forceinline__ void cmac(float2& y, float2 v, float2 h) {
+    y.x = fmaf(v.x, h.x, fmaf(-v.y, h.y, y.x));
+    y.y = fmaf(v.x, h.y, fmaf(v.y, h.x, y.y));
+}
+__device__ __forceinline__ void rmac(float2& y, float2 v, float2 h) {
+    y.x = fmaf(v.x, h.x, y.x);
+    y.y = fmaf(v.x, h.y, y.y);
 }
 
+template <bool PD>
+__global__ void __launch_bounds__(256)
+    convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
+                               const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
+                               int tap_start, int64_t M, int center, int D, int nd, int row, int taps_in_smem,
+                               const float2* __restrict__ demod, float2* __restrict__ out) {
+    extern __shared__ float2 smem[];
+    float2* seg = smem;                               // [D][row]
+    const float2* tp = taps_pm;                       // phase-major taps (shared memory when they fit)
+    const int line = blockIdx.y;
+    const int per_cta = blockDim.x * CONV_K;
+    const int m0 = blockIdx.x * per_cta;
+    const int tid = threadIdx.x;
+    if (taps_in_smem) {
+        float2* t = smem + (size_t)D * row;
+        const int ntaps_pm = __ldg(ph_off + D);
+        for (int i = tid; i < ntaps_pm; i += blockDim.x) t[i] = __ldg(taps_pm + i);
+        tp = t;
+    }
+    // bins index of segment element q = col * D + ph: j = (jbase + q) mod M, M a
+    // power of two (next_power_of_two, fft.cpp:80-82), so the wrap is a mask
+    const int64_t k0 = (int64_t)center + (int64_t)m0 * D;
+    const int64_t jbase = k0 - tap_start - (W - 1);
+    const long long mmask = (long long)M - 1;
+    const int stride = PD ? 2 : 1;
+    const long long* lb = (const long long*)bins + (int64_t)line * ns * stride;
+    // each thread stages the D consecutive bins of a column (one or two cache
+    // lines, read once), writing one element of every phase row
+    for (int col = tid; col < row; col += blockDim.x) {
+        const long long j0 = jbase + (long long)col * D;
+        for (int ph = 0; ph < D; ph++) {
+            const long long j = (j0 + ph) & mmask;
+            float2 v = make_float2(0.0f, 0.0f);
+            if (j < ns) {
+                if (PD) {
+                    const longlong2 q = __ldg(reinterpret_cast<const longlong2*>(lb) + j);
+                    v.x = __ll2float_rn(q.x) * inv_scale;
+                    v.y = __ll2float_rn(q.y) * inv_scale;
+                } else {
+                    v.x = __ll2float_rn(__ldg(lb + j)) * inv_scale;
+                }
+            }
+            seg[ph * row + col] = v;
+        }
+    }
+    __syncthreads();
+    float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
+    const int base = tid * CONV_K;
+    for (int ph = 0; ph < D; ph++) {
+        const float2* r = seg + ph * row + base;
+        const int t_beg = __ldg(ph_off + ph), t_end = __ldg(ph_off + ph + 1);
+        float2 w0 = r[0], w1 = r[1], w2 = r[2], w3;
+        const float2* hp = tp + t_beg;
+        for (int t = 0; t < t_end - t_beg; t += 4) {
+            float2 h;
+            w3 = r[t + 3]; h = hp[t];
+            if (PD) { cmac(y0, w0, h); cmac(y1, w1, h); cmac(y2, w2, h); cmac(y3, w3, h); }
+            else { rmac(y0, w0, h); rmac(y1, w1, h); rmac(y2, w2, h); rmac(y3, w3, h); }
+            w0 = r[t + 4]; h = hp[t + 1];
+            if (PD) { cmac(y0, w1, h); cmac(y1, w2, h); cmac(y2, w3, h); cmac(y3, w0, h); }
+            else { rmac(y0, w1, h); rmac(y1, w2, h); rmac(y2, w3, h); rmac(y3, w0, h); }
+            w1 = r[t + 5]; h = hp[t + 2];
+            if (PD) { cmac(y0, w2, h); cmac(y1, w3, h); cmac(y2, w0, h); cmac(y3, w1, h); }
+            else { rmac(y0, w2, h); rmac(y1, w3, h); rmac(y2, w0, h); rmac(y3, w1, h); }
+            w2 = r[t + 6]; h = hp[t + 3];
+            if (PD) { cmac(y0, w3, h); cmac(y1, w0, h); cmac(y2, w1, h); cmac(y3, w2, h); }
+            else { rmac(y0, w3, h); rmac(y1, w0, h); rmac(y2, w1, h); rmac(y3, w2, h); }
+        }
+    }
+    const float2 ys[CONV_K] = {y0, y1, y2, y3};
+#pragma unroll
+    for (int k = 0; k < CONV_K; k++) {
+        const int m = m0 + base + k;
+        if (m < nd) {
+            const float2 dm = __ldg(demod + m);
+            out[(int64_t)line * nd + m] = make_float2(ys[k].x * dm.x - ys[k].y * dm.y, ys[k].x * dm.y + ys[k].y * dm.x);
+        }
+    }
+}
+
+// Shared-memory row length for a block of `threads` threads: the elements a
+// phase row needs (threads*4 + its padded tap count + 3 for the last window),
+// padded by one element against bank conflicts.
+static int conv_row(int threads, int max_ph_taps) { return threads * CONV_K + max_ph_taps + 4 + 1; }
+
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
-                                       float inv_scale, const float2* taps, int num_taps, int tap_start, int64_t M,
-                                       int center, int decimation, int nd, const float2* demod, float2* out,
-                                       cudaStream_t stream) {
+                                       float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
+                                       int max_ph_taps, int W, int tap_start, int64_t M, int center, int decimation,
+                                       int nd, const float2* demod, float2* out, cudaStream_t stream) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
-    const int seg_len = (OUT_PER_CTA - 1) * decimation + num_taps;
-    const int row = (seg_len + decimation - 1) / decimation;
-    const size_t smem = (size_t)row * decimation * sizeof(float2);
-    dim3 grid((unsigned)((nd + OUT_PER_CTA - 1) / OUT_PER_CTA), (unsigned)num_lines);
+    // smaller blocks for few lines, so that the grid still fills the GPU
+    int threads = 128;
+    while (threads > 32 && (int64_t)num_lines * ((nd + threads * CONV_K - 1) / (threads * CONV_K)) < 2 * 152) threads /= 2;
+    int row = conv_row(threads, max_ph_taps);
+    size_t smem = ((size_t)row * decimation + (size_t)ntaps_pm) * sizeof(float2);
+    int taps_in_smem = 1;
+    const size_t limit = 200 * 1024;
+    if (smem > limit) {   // very long windows: taps from global memory (broadcast loads)
+        taps_in_smem = 0;
+        smem = (size_t)row * decimation * sizeof(float2);
+    }
+    while (smem > limit && threads > 32) {
+        threads /= 2;
+        row = conv_row(threads, max_ph_taps);
+        smem = ((size_t)row * decimation + (taps_in_smem ? (size_t)ntaps_pm : 0)) * sizeof(float2);
+    }
+    if (smem > limit) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)((nd + threads * CONV_K - 1) / (threads * CONV_K)), (unsigned)num_lines);
     if (phase_delay) {
         auto k = convolve_demodulate_kernel<true>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<grid, OUT_PER_CTA, smem, stream>>>(bins, ns, inv_scale, taps, num_taps, tap_start, M, center,
-                                               decimation, nd, demod, out);
+        k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
+                                           nd, row, taps_in_smem, demod, out);
     } else {
         auto k = convolve_demodulate_kernel<false>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<grid, OUT_PER_CTA, smem, stream>>>(bins, ns, inv_scale, taps, num_taps, tap_start, M, center,
-                                               decimation, nd, demod, out);
+        k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
+                                           nd, row, taps_in_smem, demod, out);
     }
     return cudaGetLastError();
+}
+
+int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph) {
+    int n = 0, mx = 0;
+    for (int ph = 0; ph < D; ph++) {
+        off[ph] = n;
+        const int cnt = ph <= W - 1 ? (W - 1 - ph) / D + 1 : 0;
+        const int pad = (cnt + 3) / 4 * 4;
+        for (int t = 0; t < pad; t++) out[n + t] = t < cnt ? taps[W - 1 - (ph + t * D)] : make_float2(0.0f, 0.0f);
+        n += pad;
+        mx = pad > mx ? pad : mx;
+    }
+    off[D] = n;
+    *max_ph = mx;
+    return n;
 }
 
 }  // namespace bcsim_gb300

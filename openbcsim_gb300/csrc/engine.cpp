@@ -167,6 +167,9 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
         if (!(v >= 0.0 && v < 1.0)) throw SimError(BCSIM_E_INVALID, "fir_tail_energy must be in [0, 1)");
         if (v != fir_tail_) tables_valid_ = false;
         fir_tail_ = v;
+    } else if (key == "wide_cta") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        wide_cta_ = b;
     } else if (key == "record_cache") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         record_cache_ = b;
@@ -211,6 +214,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "tile_lines") return std::to_string(tile_lines_);
     if (key == "cull") return cull_ ? "on" : "off";
     if (key == "record_cache") return record_cache_ ? "on" : "off";
+    if (key == "wide_cta") return wide_cta_ ? "on" : "off";
     if (key == "autotune") return autotune_ ? "on" : "off";
     if (key == "fir_taps") return std::to_string(tap_count_);
     throw SimError(BCSIM_E_INVALID, "Illegal key: " + key);
@@ -437,9 +441,7 @@ void Simulator::prepare_excitation_tables() {
             const int64_t n = ((tap_start_ + w) % M_ + M_) % M_;
             taps[w] = make_float2((float)ha[n].real(), (float)ha[n].imag());
         }
-        taps_dev_.reserve(taps.size() * sizeof(float2));
-        BCSIM_CUDA(cudaMemcpyAsync(taps_dev_.get(), taps.data(), taps.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
-        BCSIM_CUDA(cudaStreamSynchronize(stream_));
+        fir_taps_host_ = taps;
         fir_key_taps_ = taps_;
         fir_key_M_ = M_;
         fir_key_tail_ = fir_tail_;
@@ -449,6 +451,15 @@ void Simulator::prepare_excitation_tables() {
     const auto dm = demod_factors(fd_, fs_, decimation_, nd_, mode_ == MODE_REFERENCE);
     demod_dev_.reserve(dm.size() * sizeof(float2));
     BCSIM_CUDA(cudaMemcpyAsync(demod_dev_.get(), dm.data(), dm.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
+    // the window's taps in the kernel's phase-major order for this decimation
+    std::vector<float2> pm((size_t)tap_count_ + 4 * decimation_);
+    std::vector<int> off((size_t)decimation_ + 1);
+    ntaps_pm_ = make_phase_major_taps(fir_taps_host_.data(), (int)tap_count_, decimation_, pm.data(), off.data(),
+                                      &max_ph_taps_);
+    taps_pm_dev_.reserve(std::max<size_t>(1, (size_t)ntaps_pm_) * sizeof(float2));
+    ph_off_dev_.reserve(off.size() * sizeof(int));
+    BCSIM_CUDA(cudaMemcpyAsync(taps_pm_dev_.get(), pm.data(), (size_t)ntaps_pm_ * sizeof(float2), cudaMemcpyHostToDevice, stream_));
+    BCSIM_CUDA(cudaMemcpyAsync(ph_off_dev_.get(), off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
     tables_valid_ = true;
 }
@@ -673,6 +684,7 @@ void Simulator::prepare() {
     S = std::max(-100, std::min(100, S));
     p.log2scale = S;
     p.scale = std::ldexp(1.0f, S);
+    p.wide_cta = wide_cta_ ? 1 : 0;
     // exact culling ranges (fp64 mode): outside them the weight is exactly 0
     if (mode_ == MODE_FP64 && cull_) {
         double llo, lhi, elo, ehi;
@@ -952,8 +964,9 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     // convolution + demodulation + decimation
     timer.restart();
     BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -p.log2scale),
-                                          taps_dev_.as<float2>(), (int)tap_count_, (int)tap_start_, M_, center_,
-                                          decimation_, (int)nd_, demod_dev_.as<float2>(), dev_out, st));
+                                          taps_pm_dev_.as<float2>(), ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_,
+                                          (int)tap_count_, (int)tap_start_, M_, center_, decimation_, (int)nd_,
+                                          demod_dev_.as<float2>(), dev_out, st));
     if (timing) {
         debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
         debug_["total_ms"].push_back(total.stop());

@@ -163,6 +163,7 @@ private:
     bool cull_ = true;     // exact culling of zero-weight (scatterer, line-slot) pairs
     bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
     bool autotune_ = false;
+    bool wide_cta_ = true;       // shared-origin kernel launch shape (see launch_project_shared)
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
     uint64_t data_version_ = 1;  // bumped by every scatterer change
     uint64_t records_key_ = 0;
@@ -206,7 +207,9 @@ private:
     std::vector<float> fir_key_taps_;   // inputs of the current FIR window
     int64_t fir_key_M_ = -1;
     double fir_key_tail_ = -1.0;
-    DeviceBuffer taps_dev_, demod_dev_;
+    DeviceBuffer demod_dev_, taps_pm_dev_, ph_off_dev_;
+    std::vector<float2> fir_taps_host_;   // the FIR window taps, in window order
+    int ntaps_pm_ = 0, max_ph_taps_ = 0;
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;
     std::vector<int> line_rank_;   // position of each line in the direction-ordered sequence

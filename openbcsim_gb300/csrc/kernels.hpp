@@ -52,6 +52,7 @@ struct SimParams {
     int cull;
     float cull_l_lo, cull_l_hi, cull_e_lo, cull_e_hi;
     float cull_rho_per_bin;    // upper bound of 1 / (2 fs / c)
+    int wide_cta;              // shared-origin kernel: one 768-thread CTA per SM
 };
 
 // Frame spread of a slot of 32 lines (consecutive in the kernel's line order):
@@ -137,10 +138,19 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
 
 // Fused convolution with the analytic pulse (direct FIR over a tap window),
 // IQ demodulation and radial decimation, from fixed-point bins to complex64.
+// taps_pm/ph_off: the window's taps in phase-major order for this decimation
+// (see make_phase_major_taps), ntaps_pm = ph_off[D], max_ph_taps = the longest
+// phase.
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
-                                       float inv_scale, const float2* taps, int num_taps, int tap_start,
-                                       int64_t M, int center, int decimation, int nd, const float2* demod,
-                                       float2* out, cudaStream_t stream);
+                                       float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
+                                       int max_ph_taps, int num_taps, int tap_start, int64_t M, int center,
+                                       int decimation, int nd, const float2* demod, float2* out, cudaStream_t stream);
+
+// Host: the FIR window taps[0..W) rearranged for the convolution kernel:
+// phase ph (0..D-1) holds, for t = 0, 1, ..., the tap w = W - 1 - (ph + t*D),
+// zero-padded to a multiple of 4.  out/off must hold W + 4*D and D + 1 entries.
+// Returns the total count; *max_ph receives the longest padded phase.
+int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph);
 
 // Radix sort of (key, value) pairs: key bits [0, end_bit).  temp == nullptr
 // queries the scratch size into *temp_bytes.

@@ -45,7 +45,10 @@ constexpr size_t NA_IDS_OFF = NA_LINES_OFF + NA_MAX_LINES * sizeof(LineGeom);
 constexpr size_t NA_TILES_OFF = NA_IDS_OFF + NA_MAX_LINES * sizeof(int);
 constexpr size_t NA_TAPS_OFF = NA_TILES_OFF + NA_MAX_LINES * sizeof(LineTile);
 constexpr int NA_MAX_TAPS = 32768;
-constexpr size_t NA_DEMOD_OFF = NA_TAPS_OFF + NA_MAX_TAPS * sizeof(float2);
+constexpr int NA_MAX_DEC = 1024;                                 // radial decimation
+constexpr size_t NA_PM_OFF = NA_TAPS_OFF + NA_MAX_TAPS * sizeof(float2);              // phase-major taps
+constexpr size_t NA_PHOFF_OFF = NA_PM_OFF + (NA_MAX_TAPS + 4 * NA_MAX_DEC) * sizeof(float2);  // phase offsets
+constexpr size_t NA_DEMOD_OFF = NA_PHOFF_OFF + 4096 * sizeof(int);
 constexpr int NA_MAX_OUT = 65536;                                // decimated samples per line
 constexpr size_t NA_TOTAL = NA_DEMOD_OFF + NA_MAX_OUT * sizeof(float2);
 constexpr int NA_MAX_FFT = 65536;                                // convolution length M
@@ -63,6 +66,8 @@ void* g_na_ptr[64];          // device address of the scratch, per device (set-u
 std::complex<double> g_fft[NA_MAX_FFT];
 double g_energy[NA_MAX_FFT];
 float2 g_taps[NA_MAX_TAPS];
+float2 g_taps_pm[NA_MAX_TAPS + 4 * NA_MAX_DEC];
+int g_ph_off[NA_MAX_DEC + 1];
 float2 g_demod[NA_MAX_OUT];
 LineGeom g_lines[NA_MAX_LINES];
 int g_ids[NA_MAX_LINES];
@@ -112,6 +117,8 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
     if (num_lines < 1 || num_lines > NA_MAX_LINES)
         return fail(err, err_cap, BCSIM_E_CAPACITY, "num_lines must be in [1, 4096] for the allocation-free entry point");
     if (radial_decimation < 1) return fail(err, err_cap, BCSIM_E_INVALID, "illegal radial decimation value");
+    if (radial_decimation > NA_MAX_DEC)
+        return fail(err, err_cap, BCSIM_E_CAPACITY, "radial decimation above 1024 for the allocation-free entry point");
     if (sound_speed <= 0) return fail(err, err_cap, BCSIM_E_INVALID, "illegal sound speed");
     if (num_taps < 1) return fail(err, err_cap, BCSIM_E_INVALID, "excitation has no samples");
     if (!(amplitude_sum_bound >= 0.0f) || !std::isfinite(amplitude_sum_bound))
@@ -196,6 +203,8 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
         const std::complex<double> h = g_fft[((a + w) % M + M) % M];
         g_taps[w] = make_float2((float)h.real(), (float)h.imag());
     }
+    int max_ph = 0;
+    const int n_pm = make_phase_major_taps(g_taps, (int)W, radial_decimation, g_taps_pm, g_ph_off, &max_ph);
     const double nf = (double)demod_freq / (double)fs;
     for (int64_t m = 0; m < nd; m++) {
         const double ph = -6.283185307179586 * nf * (double)(m * radial_decimation);
@@ -235,23 +244,26 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
     LineGeom* dl = reinterpret_cast<LineGeom*>(base + NA_LINES_OFF);
     int* dids = reinterpret_cast<int*>(base + NA_IDS_OFF);
     LineTile* dtiles = reinterpret_cast<LineTile*>(base + NA_TILES_OFF);
-    float2* dtaps = reinterpret_cast<float2*>(base + NA_TAPS_OFF);
     float2* ddemod = reinterpret_cast<float2*>(base + NA_DEMOD_OFF);
+    float2* dpm = reinterpret_cast<float2*>(base + NA_PM_OFF);
+    int* dphoff = reinterpret_cast<int*>(base + NA_PHOFF_OFF);
     cudaError_t e = cudaSuccess;
     if (e == cudaSuccess) e = cudaMemcpyAsync(dl, g_lines, num_lines * sizeof(LineGeom), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dids, g_ids, num_lines * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dtiles, g_tiles, num_tiles * sizeof(LineTile), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dtaps, g_taps, W * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ddemod, g_demod, nd * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dpm, g_taps_pm, n_pm * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dphoff, g_ph_off, (radial_decimation + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(bins, 0, (size_t)num_lines * ns * stride * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
         e = launch_project_generic(static_cast<const float4*>(d_xyza), nullptr, nullptr, n, 0, 0, nullptr, nullptr, 0,
                                    dl, dids, dtiles, num_tiles, nullptr, p, b, bins, st);
     if (e == cudaSuccess)
-        e = launch_convolve_demodulate(bins, num_lines, (int)ns, p.phase_delay, std::ldexp(1.0f, -S), dtaps, (int)W,
-                                       (int)a, M, center_index, radial_decimation, (int)nd, ddemod,
-                                       static_cast<float2*>(d_out), st);
+        e = launch_convolve_demodulate(bins, num_lines, (int)ns, p.phase_delay, std::ldexp(1.0f, -S), dpm, dphoff,
+                                       n_pm, max_ph, (int)W, (int)a, M, center_index, radial_decimation, (int)nd,
+                                       ddemod, static_cast<float2*>(d_out), st);
     // the host tables above are reused by the next call: make sure they were consumed
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return fail(err, err_cap, BCSIM_E_CUDA, cudaGetErrorString(e));

@@ -370,8 +370,8 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
 //      records there), an integer atomic for the chunk's first and last bin.
 // Skipped records contribute exactly 0, so the result is bit-identical to
 // walking every record (cull=off), and does not depend on the chunk size.
-template <bool PD, int BEAM, bool REF>
-__global__ void __launch_bounds__(256, 3)
+template <bool PD, int BEAM, bool REF, int THREADS>
+__global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
     project_shared_kernel(const float4* __restrict__ records, int64_t plane, const int* __restrict__ counts, int chunk,
                           const LineGeom* __restrict__ lines, const int* __restrict__ line_order,
                           const SlotCone* __restrict__ cones, int L, unsigned long long* __restrict__ bins,
@@ -867,7 +867,17 @@ static cudaError_t launch_shared_t(const float4* records, int64_t plane, const i
     if (chunk > 1024 || chunk % FOLD) return cudaErrorInvalidValue;
     const size_t smem = 2 * (size_t)chunk * sizeof(float4);
     const int64_t chunks = (n + chunk - 1) / chunk;
-    auto k = project_shared_kernel<PD, BEAM, REF>;
+    if (p.wide_cta && L >= 768) {
+        // one 768-thread CTA per SM: all warps of an SM share one record chunk and
+        // the lookup-table planes it touches
+        auto k = project_shared_kernel<PD, BEAM, REF, 768>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<(unsigned)chunks, 768, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
+                                                   p, b);
+        return cudaGetLastError();
+    }
+    auto k = project_shared_kernel<PD, BEAM, REF, 256>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
