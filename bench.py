@@ -15,8 +15,10 @@ convolution, demodulation, decimation).  Prints one JSON line on rank 0.
 * e2e: the same metric through the C ABI with host buffers: every step uploads
   the scatterers from pinned host memory (bcsim_set_fixed_scatterers) and reads
   the IQ back (bcsim_simulate_lines), host wall clock.
-* roofline: the projection kernel against the FP32 pipe (the survey's
-  per-projection flop count; see flops_per_projection) and its HBM traffic.
+* roofline: the projection kernel against the FP32 pipe: the per-projection
+  flop count (flops_per_projection) times the pairs the kernel visits (counted
+  by one instrumented run outside the timed region; the exact slot masks skip
+  pairs of weight 0), and its HBM traffic.
 * cpu_baseline: the CPU port of the reference algorithm (oracle, reference float
   arithmetic, FFT convolution) on all host cores, on a subset of the lines.
 
@@ -43,17 +45,20 @@ METRIC = "scatterer-line projections/s"
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
-def flops_per_projection(lut: bool, phase_delay: bool) -> float:
+def flops_per_projection(lut: bool, phase_delay: bool, spline_degree=None) -> float:
     """Algorithmic FP32 flops of one scatterer-line projection (FMA = 2):
     offset (3) + three dot products (15) + distance (5) + bin index (3) +
     Gaussian exponent (5) + amplitude (1) + accumulation (2) = 34; a lookup-table
     beam replaces the Gaussian exponent by 3 normalisations and 7 trilinear
-    lerps (27); the sub-sample phase adds 6."""
+    lerps (27); the sub-sample phase adds 6; a spline scatterer adds its
+    position, 3 FMAs per non-zero basis function (6 (p+1))."""
     f = 34.0
     if lut:
         f += 27.0 - 5.0
     if phase_delay:
         f += 6.0
+    if spline_degree is not None:
+        f += 6.0 * (spline_degree + 1)
     return f
 
 
@@ -193,6 +198,7 @@ def run_gpu(args):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     proj_ms = []
+    stage = {}
     clocks = ClockSampler(local)
     clocks.start()
     if world > 1:
@@ -208,6 +214,9 @@ def run_gpu(args):
         ends[i].synchronize()
         proj_ms.append(sim.get_debug_data("fixed_projection_kernel_ms")[-1] if job.fixed else
                        sim.get_debug_data("spline_projection_kernel_ms")[-1])
+        for k in STAGE_KEYS:
+            if _has(sim, k):
+                stage.setdefault(k, []).append(sim.get_debug_data(k)[-1])
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     if world > 1:
@@ -222,17 +231,28 @@ def run_gpu(args):
     projections = job.projections
     value = projections * args.steps * world / total_s
 
+    launches_per_step = int(sim.get_debug_data("kernel_launches")[0])
+
     # ---- e2e through the C ABI with pinned host buffers ----
-    host_in = [torch.empty(f.xyza.shape, dtype=torch.float32, pin_memory=True) for f in job.fixed]
-    for h, f in zip(host_in, job.fixed):
-        h.numpy()[:] = f.xyza
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[:] = a
+        return t.numpy()
+
+    host_in = [pinned(f.xyza) for f in job.fixed]
+    host_sp = [(sp.degree, pinned(sp.knots), pinned(sp.control_points), pinned(sp.amplitudes)) for sp in job.splines]
     host_out = torch.empty((L, nd), dtype=torch.complex64, pin_memory=True)
     out_np = host_out.numpy()
 
     def e2e_step():
+        # the phantom is uploaded every step (a fresh frame), the IQ read back
         sim.clear_fixed_scatterers()
         for h in host_in:
-            sim.add_fixed_scatterers(h.numpy())
+            sim.add_fixed_scatterers(h)
+        if host_sp:
+            sim.clear_spline_scatterers()
+            for deg, kn, cp, am in host_sp:
+                sim.add_spline_scatterers(deg, kn, cp, am)
         sim.simulate_lines_line_major(out_np)
 
     for _ in range(max(1, args.warmup)):
@@ -249,15 +269,32 @@ def run_gpu(args):
         t = torch.tensor([e2e_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_total = float(t.item())
-    h2d = sum(f.xyza.nbytes for f in job.fixed)
+    h2d = sum(h.nbytes for h in host_in) + sum(kn.nbytes + cp.nbytes + am.nbytes for _, kn, cp, am in host_sp)
     d2h = L * nd * 8
+
+    # ---- one instrumented run (outside every timed region): the (record, line)
+    # pairs the shared-origin kernel visits and those with a non-zero weight ----
+    shared_path = "prep_sort_ms" in stage
+    visited = nonzero = None
+    if shared_path:
+        sim.set_parameter("count_pairs", "on")
+        sim.simulate_lines_device(dev_out.data_ptr(), dev_out.numel())
+        torch.cuda.synchronize()
+        visited = int(sim.get_debug_data("evaluated_pairs")[0])
+        nonzero = int(sim.get_debug_data("weighted_pairs")[0])
+        sim.set_parameter("count_pairs", "off")
 
     if rank != 0:
         return None
     lut = not hasattr(job.beam, "sigma_lateral")
-    fpp = flops_per_projection(lut, job.phase_delay)
+    fpp = flops_per_projection(lut, job.phase_delay, job.splines[0].degree if job.splines and not job.fixed else None)
     proj_avg_ms = statistics.mean(proj_ms)
-    achieved_tflops = projections * fpp / (proj_avg_ms / 1e3) / 1e12
+    # units one launch processes: the pairs the shared-origin kernel visits (the
+    # others have weight exactly 0 and are skipped by the slot masks); the
+    # per-pair kernel evaluates every (scatterer, line) pair
+    units = visited if visited is not None else projections
+    achieved_tflops = units * fpp / (proj_avg_ms / 1e3) / 1e12
+    all_pairs_tflops = projections * fpp / (proj_avg_ms / 1e3) / 1e12
     sms = sm_count()
     clock_mhz = clk.get("sm_mhz") or 2070.0
     fp32_peak = sms * 128 * 2 * clock_mhz * 1e6 / 1e12
@@ -266,7 +303,10 @@ def run_gpu(args):
         with open(MEASURED_PEAKS) as f:
             peaks = json.load(f)
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    alg_bytes = sum(f.xyza.nbytes for f in job.fixed) + (job.beam.samples.nbytes if lut else 0) + L * nd * 8
+    # phantom (16 B per fixed scatterer, 12 K + 4 B per spline scatterer) + table + IQ
+    alg_bytes = (sum(f.xyza.nbytes for f in job.fixed) +
+                 sum(sp.control_points.shape[0] * (12 * sp.control_points.shape[1] + 4) for sp in job.splines) +
+                 (job.beam.samples.nbytes if lut else 0) + L * nd * 8)
     traffic = None
     if args.traffic_bytes:
         traffic = float(args.traffic_bytes)
@@ -274,7 +314,7 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "projections/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)", "data": "synthetic (seeded)",
-        "config": {"workload": f"{job.name}: {job.num_scatterers} fixed scatterers x {L} lines, "
+        "config": {"workload": f"{job.name}: {job.num_scatterers} {'fixed' if job.fixed else 'spline'} scatterers x {L} lines, "
                                f"{'256x64x64 LUT beam' if lut else 'Gaussian beam'}, ns={job.num_samples}, "
                                f"decimation {job.decimation}, phase delay {'on' if job.phase_delay else 'off'}",
                    "projections_per_step": projections, "l2": "flushed between steps (512 MiB memset)",
@@ -282,25 +322,35 @@ def run_gpu(args):
         "e2e": {"value": projections * args.steps * world / e2e_total, "unit": "projections/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_total * 1e3 / args.steps},
-        "roofline": {"bound": "fp32", "kernel": "project_shared_kernel",
+        "roofline": {"bound": "fp32", "kernel": "project_shared_kernel" if shared_path else "project_generic_kernel",
                      "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tflops / fp32_peak, "traffic": traffic,
-                     "flops_per_projection": fpp, "kernel_ms": proj_avg_ms,
+                     "flops_per_unit": fpp, "units_per_launch": units,
+                     "unit_counted": "visited (record, line) pairs" if shared_path else "(scatterer, line) pairs",
+                     "pairs": {"all": projections, "visited": visited, "nonzero_weight": nonzero},
+                     "all_pairs_convention": {"achieved": all_pairs_tflops, "frac": all_pairs_tflops / fp32_peak,
+                                              "note": "flops_per_unit x N x L: counts the pairs of weight exactly 0 "
+                                                      "that the slot masks skip, so it can exceed the peak"},
+                     "kernel_ms": proj_avg_ms,
                      "peak_source": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {clock_mhz:.0f} MHz "
                                     "(median SM clock sampled during the timed steps)"},
         "roofline_hbm": {"achieved": alg_bytes / (proj_avg_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
                          "frac": alg_bytes / (proj_avg_ms / 1e3) / 1e9 / hbm_peak,
                          "algorithmic_bytes": alg_bytes, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
         "clocks": clk,
-        "gpu_launches": args.steps * 8,
-        "stage_ms": {k: statistics.mean(sim.get_debug_data(k)) for k in
-                     ["kernel_memset_ms", "prep_sort_ms", "fixed_projection_kernel_ms",
-                      "kernel_convolve_demodulate_ms", "total_ms"] if _has(sim, k)},
+        "gpu_launches": args.steps * launches_per_step,
+        "gpu_launches_note": f"{launches_per_step} kernels of this library per step (the CUB radix sort of the "
+                             "shared-origin path launches its own kernels in addition)",
+        "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
         "wall_s": wall,
     }
     if not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(job, args.cpu_seconds)
     return result
+
+
+STAGE_KEYS = ["kernel_memset_ms", "prep_sort_ms", "fixed_projection_kernel_ms", "spline_projection_kernel_ms",
+              "kernel_convolve_demodulate_ms", "total_ms"]
 
 
 def _has(sim, key):

@@ -18,12 +18,17 @@
 // of output m, row q mod D holds the elements of one phase, so that a phase's
 // taps walk along one row.  Each thread computes 4 consecutive outputs; along a
 // row they need consecutive elements, held in a rotating window of 4 registers:
-// one shared-memory load and one (broadcast) tap load per 16 complex MACs.  The
-// taps are stored phase-major on the host, zero-padded to a multiple of 4 per
-// phase.
+// one shared-memory load and one (broadcast) tap load per 16 complex MACs.  A
+// row is stored as 4 sub-rows by element index mod 4 (element e at sub-row e&3,
+// position e>>2), so that the 32 threads of a warp, whose windows start 4
+// elements apart, read 32 consecutive elements of one sub-row (no bank
+// conflicts); sub-rows are padded to 4 mod 16 elements so that the staging
+// stores, which cover all four sub-rows, do not conflict either.  The taps are
+// stored phase-major on the host, zero-padded to a multiple of 4 per phase.
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "kernels.hpp"
+#include "fixedpoint.cuh"
 
 namespace bcsim_gb300 {
 
@@ -42,10 +47,11 @@ template <bool PD>
 __global__ void __launch_bounds__(256)
     convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
                                const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
-                               int tap_start, int64_t M, int center, int D, int nd, int row, int taps_in_smem,
-                               const float2* __restrict__ demod, float2* __restrict__ out) {
+                               int tap_start, int64_t M, int center, int D, int nd, int sub, int cols,
+                               int taps_in_smem, const float2* __restrict__ demod, float2* __restrict__ out) {
     extern __shared__ float2 smem[];
-    float2* seg = smem;                               // [D][row]
+    float2* seg = smem;                               // [D][4][sub]
+    const int row = 4 * sub;
     const float2* tp = taps_pm;                       // phase-major taps (shared memory when they fit)
     const int line = blockIdx.y;
     const int per_cta = blockDim.x * CONV_K;
@@ -66,48 +72,53 @@ __global__ void __launch_bounds__(256)
     const long long* lb = (const long long*)bins + (int64_t)line * ns * stride;
     // each thread stages the D consecutive bins of a column (one or two cache
     // lines, read once), writing one element of every phase row
-    for (int col = tid; col < row; col += blockDim.x) {
+    for (int col = tid; col < cols; col += blockDim.x) {
         const long long j0 = jbase + (long long)col * D;
+        float2* dst = seg + (col & 3) * sub + (col >> 2);
         for (int ph = 0; ph < D; ph++) {
             const long long j = (j0 + ph) & mmask;
             float2 v = make_float2(0.0f, 0.0f);
             if (j < ns) {
                 if (PD) {
                     const longlong2 q = __ldg(reinterpret_cast<const longlong2*>(lb) + j);
-                    v.x = __ll2float_rn(q.x) * inv_scale;
-                    v.y = __ll2float_rn(q.y) * inv_scale;
+                    v.x = ll2f_rn(q.x) * inv_scale;
+                    v.y = ll2f_rn(q.y) * inv_scale;
                 } else {
-                    v.x = __ll2float_rn(__ldg(lb + j)) * inv_scale;
+                    v.x = ll2f_rn(__ldg(lb + j)) * inv_scale;
                 }
             }
-            seg[ph * row + col] = v;
+            dst[ph * row] = v;
         }
     }
     __syncthreads();
     float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
-    const int base = tid * CONV_K;
     for (int ph = 0; ph < D; ph++) {
-        const float2* r = seg + ph * row + base;
+        // element tid*4 + t + j of the phase row: sub-row j & 3, position tid + t/4 + j/4
+        const float2* r0 = seg + ph * row + tid;
+        const float2* r1 = r0 + sub;
+        const float2* r2 = r1 + sub;
+        const float2* r3 = r2 + sub;
         const int t_beg = __ldg(ph_off + ph), t_end = __ldg(ph_off + ph + 1);
-        float2 w0 = r[0], w1 = r[1], w2 = r[2], w3;
+        float2 w0 = r0[0], w1 = r1[0], w2 = r2[0], w3;
         const float2* hp = tp + t_beg;
-        for (int t = 0; t < t_end - t_beg; t += 4) {
+        for (int t = 0, i = 0; t < t_end - t_beg; t += 4, i++) {
             float2 h;
-            w3 = r[t + 3]; h = hp[t];
+            w3 = r3[i]; h = hp[t];
             if (PD) { cmac(y0, w0, h); cmac(y1, w1, h); cmac(y2, w2, h); cmac(y3, w3, h); }
             else { rmac(y0, w0, h); rmac(y1, w1, h); rmac(y2, w2, h); rmac(y3, w3, h); }
-            w0 = r[t + 4]; h = hp[t + 1];
+            w0 = r0[i + 1]; h = hp[t + 1];
             if (PD) { cmac(y0, w1, h); cmac(y1, w2, h); cmac(y2, w3, h); cmac(y3, w0, h); }
             else { rmac(y0, w1, h); rmac(y1, w2, h); rmac(y2, w3, h); rmac(y3, w0, h); }
-            w1 = r[t + 5]; h = hp[t + 2];
+            w1 = r1[i + 1]; h = hp[t + 2];
             if (PD) { cmac(y0, w2, h); cmac(y1, w3, h); cmac(y2, w0, h); cmac(y3, w1, h); }
             else { rmac(y0, w2, h); rmac(y1, w3, h); rmac(y2, w0, h); rmac(y3, w1, h); }
-            w2 = r[t + 6]; h = hp[t + 3];
+            w2 = r2[i + 1]; h = hp[t + 3];
             if (PD) { cmac(y0, w3, h); cmac(y1, w0, h); cmac(y2, w1, h); cmac(y3, w2, h); }
             else { rmac(y0, w3, h); rmac(y1, w0, h); rmac(y2, w1, h); rmac(y3, w2, h); }
         }
     }
     const float2 ys[CONV_K] = {y0, y1, y2, y3};
+    const int base = tid * CONV_K;
 #pragma unroll
     for (int k = 0; k < CONV_K; k++) {
         const int m = m0 + base + k;
@@ -118,46 +129,48 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// Shared-memory row length for a block of `threads` threads: the elements a
-// phase row needs (threads*4 + its padded tap count + 3 for the last window),
-// padded by one element against bank conflicts.
-static int conv_row(int threads, int max_ph_taps) { return threads * CONV_K + max_ph_taps + 4 + 1; }
+// Staged elements per phase row for a block of `threads` threads: thread T's
+// window reaches element 4T + max_ph_taps + 2, so 4*threads + max_ph_taps
+// elements (max_ph_taps is a multiple of 4) cover every read.
+static int conv_cols(int threads, int max_ph_taps) { return threads * CONV_K + max_ph_taps; }
+// Sub-row length: cols/4 positions, padded to 4 mod 16.
+static int conv_sub(int threads, int max_ph_taps) {
+    const int need = conv_cols(threads, max_ph_taps) / 4;
+    return need + ((4 - need) % 16 + 16) % 16;
+}
 
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                        float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
                                        int max_ph_taps, int W, int tap_start, int64_t M, int center, int decimation,
                                        int nd, const float2* demod, float2* out, cudaStream_t stream) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
+    if (max_ph_taps % 4) return cudaErrorInvalidValue;
     // smaller blocks for few lines, so that the grid still fills the GPU
     int threads = 128;
     while (threads > 32 && (int64_t)num_lines * ((nd + threads * CONV_K - 1) / (threads * CONV_K)) < 2 * 152) threads /= 2;
-    int row = conv_row(threads, max_ph_taps);
-    size_t smem = ((size_t)row * decimation + (size_t)ntaps_pm) * sizeof(float2);
+    auto smem_for = [&](int th, int taps_smem) {
+        return ((size_t)4 * conv_sub(th, max_ph_taps) * decimation + (taps_smem ? (size_t)ntaps_pm : 0)) * sizeof(float2);
+    };
     int taps_in_smem = 1;
     const size_t limit = 200 * 1024;
-    if (smem > limit) {   // very long windows: taps from global memory (broadcast loads)
-        taps_in_smem = 0;
-        smem = (size_t)row * decimation * sizeof(float2);
-    }
-    while (smem > limit && threads > 32) {
-        threads /= 2;
-        row = conv_row(threads, max_ph_taps);
-        smem = ((size_t)row * decimation + (taps_in_smem ? (size_t)ntaps_pm : 0)) * sizeof(float2);
-    }
+    if (smem_for(threads, 1) > limit) taps_in_smem = 0;   // very long windows: taps from global memory (broadcast loads)
+    while (smem_for(threads, taps_in_smem) > limit && threads > 32) threads /= 2;
+    const size_t smem = smem_for(threads, taps_in_smem);
     if (smem > limit) return cudaErrorInvalidValue;
+    const int sub = conv_sub(threads, max_ph_taps), cols = conv_cols(threads, max_ph_taps);
     const dim3 grid((unsigned)((nd + threads * CONV_K - 1) / (threads * CONV_K)), (unsigned)num_lines);
     if (phase_delay) {
         auto k = convolve_demodulate_kernel<true>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
-                                           nd, row, taps_in_smem, demod, out);
+                                           nd, sub, cols, taps_in_smem, demod, out);
     } else {
         auto k = convolve_demodulate_kernel<false>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
-                                           nd, row, taps_in_smem, demod, out);
+                                           nd, sub, cols, taps_in_smem, demod, out);
     }
     return cudaGetLastError();
 }

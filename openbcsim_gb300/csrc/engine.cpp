@@ -170,6 +170,12 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
     } else if (key == "wide_cta") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         wide_cta_ = b;
+    } else if (key == "count_pairs") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        count_pairs_ = b;
+    } else if (key == "lut_smem") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        lut_smem_ = b;
     } else if (key == "record_cache") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         record_cache_ = b;
@@ -215,6 +221,8 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "cull") return cull_ ? "on" : "off";
     if (key == "record_cache") return record_cache_ ? "on" : "off";
     if (key == "wide_cta") return wide_cta_ ? "on" : "off";
+    if (key == "lut_smem") return lut_smem_ ? "on" : "off";
+    if (key == "count_pairs") return count_pairs_ ? "on" : "off";
     if (key == "autotune") return autotune_ ? "on" : "off";
     if (key == "fir_taps") return std::to_string(tap_count_);
     throw SimError(BCSIM_E_INVALID, "Illegal key: " + key);
@@ -416,6 +424,7 @@ void Simulator::throw_if_not_configured() const {
 }
 
 std::vector<double> Simulator::get_debug_data(const std::string& key) const {
+    if (key == "kernel_launches") return {(double)last_launches_};
     auto it = debug_.find(key);
     if (it == debug_.end()) throw SimError(BCSIM_E_INVALID, "invalid debug data key: " + key);
     return it->second;
@@ -685,6 +694,7 @@ void Simulator::prepare() {
     p.log2scale = S;
     p.scale = std::ldexp(1.0f, S);
     p.wide_cta = wide_cta_ ? 1 : 0;
+    p.lut_smem = lut_smem_ ? 1 : 0;
     // exact culling ranges (fp64 mode): outside them the weight is exactly 0
     if (mode_ == MODE_FP64 && cull_) {
         double llo, lhi, elo, ehi;
@@ -814,6 +824,7 @@ void Simulator::prepare() {
     P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
     bins_.reserve(P.bins_bytes);
     counts_.reserve(4 * sizeof(int));
+    pair_counts_.reserve(2 * sizeof(unsigned long long));
     out_.reserve((size_t)L * nd_ * sizeof(float2));
     P.spline_off.assign(splines_.size(), -1);
     if (P.n_shared > 0) {
@@ -889,6 +900,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     EventTimer total(timing, st);
     EventTimer timer(timing, st);
     unsigned long long* bins = bins_.as<unsigned long long>();
+    int launches = 0;   // kernels of this library launched (the radix sort's are counted apart)
     const LineGeom* lines_d = lines_dev_.as<LineGeom>();
     BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, st));
     if (timing) debug_["kernel_memset_ms"].push_back(timer.stop());
@@ -899,11 +911,13 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
         if (!record_cache_ || records_key_ != P.records_key) {
             const float* origin = lines_[0].o;
             if (fixed_n_ > 0)
+                ++launches;
                 BCSIM_CUDA(launch_prep_shared(fixed_xyza_.as<float4>(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
                                               vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
             for (size_t d = 0; d < splines_.size(); d++) {
                 if (!P.spline_shared[d]) continue;
                 const SplineDataset& ds = splines_[d];
+                ++launches;
                 BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                                      P.spline_first_cs[d], ds.degree, spl_basis_d_.as<double>() + 64 * d,
                                                      spl_basis_f_.as<float>() + 64 * d, P.spline_off[d], origin, p, b,
@@ -913,24 +927,35 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
             size_t tmp_bytes = P.sort_tmp_bytes;
             BCSIM_CUDA(radix_sort_pairs(sort_tmp_.get(), &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
                                         vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, P.end_bit, st));
+            launches += 3;   // init, count, finish
             BCSIM_CUDA(launch_count_keys(keys_out_.as<uint32_t>(), N, ns, counts_.as<int>(), st));
+            ++launches;
             BCSIM_CUDA(launch_gather_records(vals_out_.as<uint32_t>(), counts_.as<int>(), N, recA_.as<float4>(),
                                              recB_.as<float4>(), records_.as<float4>(), N, st));
             records_key_ = P.records_key;
         }
         if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
         timer.restart();
+        unsigned long long* pair_counts = nullptr;
+        if (count_pairs_ && p.mode == MODE_FP64) {
+            pair_counts = pair_counts_.as<unsigned long long>();
+            BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 2 * sizeof(unsigned long long), st));
+        }
+        ++launches;
         BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
-                                         line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins, st));
+                                         line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins,
+                                         pair_counts, st));
         // near-origin residue, per pair
         for (const GenLaunch& g : P.gl) {
             if (g.kind == 0) {
+                ++launches;
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
                                                   vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
                                                   (int)g.num_tiles, nullptr, p, b, bins, st));
             } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
+                ++launches;
                 BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                                   ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
@@ -946,14 +971,16 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     for (const GenLaunch& g : P.gl) {
         if (g.kind == 0) {
             if (P.shared) continue;
-            BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
+            ++launches;
+                BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
                                               b, bins, st));
         } else {
             if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
-            BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+            ++launches;
+                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                               gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
@@ -963,6 +990,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
 
     // convolution + demodulation + decimation
     timer.restart();
+    ++launches;
     BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -p.log2scale),
                                           taps_pm_dev_.as<float2>(), ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_,
                                           (int)tap_count_, (int)tap_start_, M_, center_, decimation_, (int)nd_,
@@ -971,6 +999,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
         debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
         debug_["total_ms"].push_back(total.stop());
     }
+    last_launches_ = launches;
 }
 
 void Simulator::simulate(float2* dev_out, float* host_out) {
@@ -978,6 +1007,13 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     if (store_details_) debug_.clear();
     const cudaStream_t st = stream_;
     enqueue(st, dev_out, store_details_);
+    if (count_pairs_ && plan_.n_shared > 0 && mode_ == MODE_FP64) {
+        unsigned long long c[2] = {0, 0};
+        BCSIM_CUDA(cudaMemcpyAsync(c, pair_counts_.get(), sizeof c, cudaMemcpyDeviceToHost, st));
+        BCSIM_CUDA(cudaStreamSynchronize(st));
+        debug_["evaluated_pairs"] = {(double)c[0]};
+        debug_["weighted_pairs"] = {(double)c[1]};
+    }
     if (host_out) {
         EventTimer timer(store_details_, st);
         BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)num_lines_ * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
@@ -1086,6 +1122,8 @@ void Simulator::clone_from(Simulator& o) {
     cull_ = o.cull_;
     record_cache_ = o.record_cache_;
     autotune_ = o.autotune_;
+    wide_cta_ = o.wide_cta_;
+    lut_smem_ = o.lut_smem_;
     excitation_set_ = o.excitation_set_;
     taps_ = o.taps_;
     center_ = o.center_;

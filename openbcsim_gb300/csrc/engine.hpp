@@ -164,6 +164,10 @@ private:
     bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
     bool autotune_ = false;
     bool wide_cta_ = true;       // shared-origin kernel launch shape (see launch_project_shared)
+    bool lut_smem_ = true;       // wide shared-origin kernel: stage the chunk's lookup-table planes in shared memory
+    bool count_pairs_ = false;   // instrumented shared-origin kernel: visited / non-zero (record, line) pairs
+    int last_launches_ = 0;      // kernels of this library launched by the last enqueue
+    DeviceBuffer pair_counts_;
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
     uint64_t data_version_ = 1;  // bumped by every scatterer change
     uint64_t records_key_ = 0;

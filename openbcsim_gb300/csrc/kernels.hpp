@@ -52,7 +52,8 @@ struct SimParams {
     int cull;
     float cull_l_lo, cull_l_hi, cull_e_lo, cull_e_hi;
     float cull_rho_per_bin;    // upper bound of 1 / (2 fs / c)
-    int wide_cta;              // shared-origin kernel: one 768-thread CTA per SM
+    int wide_cta;              // shared-origin kernel: 1024/512-thread CTAs for >= 512 lines
+    int lut_smem;              // wide shared-origin kernel: lookup-table planes in shared memory
 };
 
 // Frame spread of a slot of 32 lines (consecutive in the kernel's line order):
@@ -118,11 +119,13 @@ cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts
 
 // Projection of the counts[0] sorted records onto all lines (lines share the
 // origin); `chunk` records per CTA, lines taken in the order line_order[] with
-// slot cones[] per 32 of them.
+// slot cones[] per 32 of them.  pair_counts (fp64 mode only; normally null):
+// when set, a counting variant adds the (record, line) pairs it visits to
+// pair_counts[0] and those with a non-zero beam weight to pair_counts[1].
 cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
                                   const LineGeom* lines, const int* line_order, const SlotCone* cones,
                                   int num_lines, const SimParams& p, const BeamDev& b, unsigned long long* bins,
-                                  cudaStream_t stream);
+                                  unsigned long long* pair_counts, cudaStream_t stream);
 
 // Per-pair projection: fixed scatterers (cps == nullptr) or splines, arbitrary
 // lines.  If index_list is given, the entries index_list[counts[0] ...

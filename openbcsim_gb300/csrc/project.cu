@@ -30,6 +30,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include "kernels.hpp"
 #include "dfloat.cuh"
+#include "fixedpoint.cuh"
 
 namespace bcsim_gb300 {
 
@@ -40,7 +41,7 @@ static constexpr double TWO_PI_LITERAL = 6.283185307179586;  // CpuAlgorithm.cpp
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void bin_add(unsigned long long* addr, float v, float scale) {
     if (v != 0.0f) {
-        const long long q = __float2ll_rn(v * scale);
+        const long long q = f2ll_rn(v * scale);
         if (q != 0) atomicAdd(addr, (unsigned long long)q);
     }
 }
@@ -370,14 +371,15 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
 //      records there), an integer atomic for the chunk's first and last bin.
 // Skipped records contribute exactly 0, so the result is bit-identical to
 // walking every record (cull=off), and does not depend on the chunk size.
-template <bool PD, int BEAM, bool REF, int THREADS>
-__global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
+template <bool PD, int BEAM, bool REF, int THREADS, bool COUNT>
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 3))
     project_shared_kernel(const float4* __restrict__ records, int64_t plane, const int* __restrict__ counts, int chunk,
                           const LineGeom* __restrict__ lines, const int* __restrict__ line_order,
                           const SlotCone* __restrict__ cones, int L, unsigned long long* __restrict__ bins,
-                          SimParams p, BeamDev b) {
+                          SimParams p, BeamDev b, int lut_planes, unsigned long long* __restrict__ pair_counts) {
     extern __shared__ __align__(128) float4 sm[];
     __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_lut_base, s_lut_planes;
     const int n_valid = __ldg(counts);
     const int64_t start = (int64_t)blockIdx.x * chunk;
     if (start >= n_valid) return;
@@ -386,17 +388,32 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
     const int lane = tid & 31;
     float4* smA = sm;
     float4* smB = sm + chunk;
+    float4* smL = sm + 2 * chunk;   // lut_planes radial planes of the packed table
+    const int lut_plane_size = b.nl * b.ne;
 
     if (tid == 0) {
         mbar_init(&bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // records are in bin order, so their radial table index r0 does not
+        // decrease within the chunk: stage the planes from the first record's on
+        int base = 0, planes = 0;
+        if (BEAM == BEAM_LUT && !REF && lut_planes > 0) {
+            base = __float_as_int(__ldg(&records[plane + start].z));
+            base = min(max(base, 0), b.nr - 1);
+            planes = min(lut_planes, b.nr - base);
+        }
+        s_lut_base = base;
+        s_lut_planes = planes;
     }
     __syncthreads();
+    const int lut_base = s_lut_base, lut_staged = s_lut_planes;
     if (tid == 0) {
         const unsigned bytes = (unsigned)cnt * sizeof(float4);
-        mbar_expect_tx(&bar, 2 * bytes);
+        const unsigned lut_bytes = (unsigned)lut_staged * (unsigned)lut_plane_size * (unsigned)sizeof(float4);
+        mbar_expect_tx(&bar, 2 * bytes + lut_bytes);
         bulk_load(smA, records + start, bytes, &bar);
         bulk_load(smB, records + plane + start, bytes, &bar);
+        if (lut_bytes) bulk_load(smL, b.lut4 + (int64_t)lut_base * lut_plane_size, lut_bytes, &bar);
     }
     if (!mbar_wait(&bar, 0, 1u << 26)) {
         g_bcsim_error_flag = 1;
@@ -415,6 +432,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
     const int nwords = (cnt + 31) >> 5;
 
     for (int g0 = 0; g0 < L; g0 += blockDim.x) {
+        if (g0 + (tid & ~31) >= L) break;   // this warp has no line in this group (nor in later ones)
         const int slot_pos = g0 + tid;
         const bool active = slot_pos < L;
         const int line = __ldg(line_order + (active ? slot_pos : L - 1));
@@ -451,28 +469,28 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
         }
 
         // ---- phase B: walk the selected records in bin order ----
+        unsigned walked = 0, weighted = 0;   // COUNT: pairs visited, pairs with a non-zero weight
         int cur = first_bin;
         long long tr = 0, ti = 0;
         float ar = 0.0f, ai = 0.0f;
-        int64_t fold_block = start / FOLD;
-        for (int w = 0; w < nwords; w++) {
-            unsigned word = cull ? __shfl_sync(0xffffffffu, mask, w) : 0xffffffffu;
-            if (!cull && w == nwords - 1 && (cnt & 31)) word &= (1u << (cnt & 31)) - 1u;
-            while (word) {
-                const int i = (w << 5) + __ffs(word) - 1;
-                word &= word - 1u;
-                const float4 B = smB[i];
-                const int idx = __float_as_int(B.w);
-                const int64_t blk = (start + i) / FOLD;
-                // fold at absolute record indices k*FOLD (chunk starts are multiples
-                // of FOLD), so the FP32 partial sums do not depend on the chunk size
-                if (idx != cur || blk != fold_block) {
-                    tr += __float2ll_rn(ar * scale);
-                    if (PD) ti += __float2ll_rn(ai * scale);
-                    ar = 0.0f;
-                    ai = 0.0f;
-                    fold_block = blk;
-                    if (idx != cur) {
+        // fold groups: FOLD records = FOLD/32 mask words; the chunk starts at a
+        // multiple of FOLD, so the FP32 run sums end at absolute record indices
+        // k*FOLD whatever the chunk size
+        for (int w0 = 0; w0 < nwords; w0 += FOLD / 32) {
+            const int w1 = min(w0 + FOLD / 32, nwords);
+            for (int w = w0; w < w1; w++) {
+                unsigned word = cull ? __shfl_sync(0xffffffffu, mask, w) : 0xffffffffu;
+                if (!cull && w == nwords - 1 && (cnt & 31)) word &= (1u << (cnt & 31)) - 1u;
+                while (word) {
+                    const int i = (w << 5) + __ffs(word) - 1;
+                    word &= word - 1u;
+                    const float4 B = smB[i];
+                    const int idx = __float_as_int(B.w);
+                    if (idx != cur) {   // warp-uniform: the record is the same for all lanes
+                        tr += f2ll_rn(ar * scale);
+                        if (PD) ti += f2ll_rn(ai * scale);
+                        ar = 0.0f;
+                        ai = 0.0f;
                         if (active) {
                             unsigned long long* dst = lb + (int64_t)cur * stride;
                             if (cur == first_bin || cur == last_bin) {
@@ -487,60 +505,90 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 512 ? 1 : 3)
                         ti = 0;
                         cur = idx;
                     }
-                }
-                const float4 A = smA[i];
-                float w8;
-                if (REF) {
-                    // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
-                    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
-                    const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
-                    const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
-                    if (BEAM == BEAM_GAUSSIAN) {
-                        w8 = gauss_weight_ref(b, l, e);
-                    } else {
-                        // the reference recomputes the radial table coordinate per pair from r
-                        w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
-                                                                   __fmul_rn(A.z, A.z))),
-                                            l, e);
-                    }
-                    w8 = signbit(dot) ? 0.0f : w8;
-                } else {
-                    const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
-                    const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
-                    const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
-                    if (BEAM == BEAM_GAUSSIAN) {
-                        w8 = exp2f(-fmaf(u, u, v * v));
-                        // arc projection: a line for which the scatterer lies behind the
-                        // origin sees it at -rho, outside [0, ns) for every record
-                        // (near-origin scatterers take the per-pair path)
+                    const float4 A = smA[i];
+                    float w8;
+                    if (REF) {
+                        // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
+                        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
+                        const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
+                        const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
+                        if (BEAM == BEAM_GAUSSIAN) {
+                            w8 = gauss_weight_ref(b, l, e);
+                        } else {
+                            // the reference recomputes the radial table coordinate per pair from r
+                            w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                                       __fmul_rn(A.z, A.z))),
+                                                l, e);
+                        }
                         w8 = signbit(dot) ? 0.0f : w8;
                     } else {
-                        w8 = 0.0f;
-                        if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
-                            const int l0 = (int)u, e0 = (int)v;
-                            const float fl = u < 0.0f ? 0.0f : u - (float)l0;
-                            const float fe = v < 0.0f ? 0.0f : v - (float)e0;
-                            const int base = (__float_as_int(B.z) * b.nl + l0) * b.ne + e0;
-                            const float4 P = __ldg(b.lut4 + base);
-                            const float4 Q = __ldg(b.lut4 + base + b.ne);
-                            const float fr = B.y;
-                            // radial, lateral, elevational (BeamProfile.cpp:116-127)
-                            const float c00 = fmaf(fr, P.z - P.x, P.x);
-                            const float c01 = fmaf(fr, P.w - P.y, P.y);
-                            const float c10 = fmaf(fr, Q.z - Q.x, Q.x);
-                            const float c11 = fmaf(fr, Q.w - Q.y, Q.y);
-                            const float c0 = fmaf(fl, c10 - c00, c00);
-                            const float c1 = fmaf(fl, c11 - c01, c01);
-                            w8 = fmaf(fe, c1 - c0, c0);
+                        const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
+                        const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
+                        const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
+                        if (BEAM == BEAM_GAUSSIAN) {
+                            w8 = exp2f(-fmaf(u, u, v * v));
+                            // arc projection: a line for which the scatterer lies behind the
+                            // origin sees it at -rho, outside [0, ns) for every record
+                            // (near-origin scatterers take the per-pair path)
+                            w8 = signbit(dot) ? 0.0f : w8;
+                        } else {
+                            w8 = 0.0f;
+                            // (a warp whose lanes all miss the table skips the lookup)
+                            if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
+                                // -1 < t < n-1: the reference's trunc-toward-zero index
+                                // with the fraction dropped for -1 < t < 0
+                                // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
+                                // integer part of max(t, 0) + 2^23 rounded down
+                                const float uc = fmaxf(u, 0.0f), vc = fmaxf(v, 0.0f);
+                                const float tu = __fadd_rd(uc, 8388608.0f), tv = __fadd_rd(vc, 8388608.0f);
+                                const int l0 = __float_as_int(tu) - 0x4B000000, e0 = __float_as_int(tv) - 0x4B000000;
+                                const float fl = uc - (tu - 8388608.0f);
+                                const float fe = vc - (tv - 8388608.0f);
+                                const int r0 = __float_as_int(B.z);
+                                const int off = l0 * b.ne + e0;
+                                float4 P, Q;
+                                if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
+                                    const float4* pl = smL + (r0 - lut_base) * lut_plane_size + off;
+                                    P = pl[0];
+                                    Q = pl[b.ne];
+                                } else {
+                                    const int base = r0 * lut_plane_size + off;
+                                    P = __ldg(b.lut4 + base);
+                                    Q = __ldg(b.lut4 + base + b.ne);
+                                }
+                                const float fr = B.y;
+                                // radial, lateral, elevational (BeamProfile.cpp:116-127)
+                                const float c00 = fmaf(fr, P.z - P.x, P.x);
+                                const float c01 = fmaf(fr, P.w - P.y, P.y);
+                                const float c10 = fmaf(fr, Q.z - Q.x, Q.x);
+                                const float c11 = fmaf(fr, Q.w - Q.y, Q.y);
+                                const float c0 = fmaf(fl, c10 - c00, c00);
+                                const float c1 = fmaf(fl, c11 - c01, c01);
+                                w8 = fmaf(fe, c1 - c0, c0);
+                            }
                         }
                     }
+                    ar = fmaf(w8, A.w, ar);
+                    if (PD) ai = fmaf(w8, B.x, ai);
+                    if (COUNT) {
+                        walked += active ? 1u : 0u;
+                        weighted += (active && w8 != 0.0f) ? 1u : 0u;
+                    }
                 }
-                ar = fmaf(w8, A.w, ar);
-                if (PD) ai = fmaf(w8, B.x, ai);
+            }
+            tr += f2ll_rn(ar * scale);
+            if (PD) ti += f2ll_rn(ai * scale);
+            ar = 0.0f;
+            ai = 0.0f;
+        }
+        if (COUNT) {
+            walked = __reduce_add_sync(0xffffffffu, walked);
+            weighted = __reduce_add_sync(0xffffffffu, weighted);
+            if (lane == 0) {
+                atomicAdd(pair_counts, (unsigned long long)walked);
+                atomicAdd(pair_counts + 1, (unsigned long long)weighted);
             }
         }
-        tr += __float2ll_rn(ar * scale);
-        if (PD) ti += __float2ll_rn(ai * scale);
         if (active) {
             unsigned long long* dst = lb + (int64_t)cur * stride;
             if (cur == first_bin || cur == last_bin) {
@@ -859,48 +907,73 @@ cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts
     return cudaGetLastError();
 }
 
-template <bool PD, int BEAM, bool REF>
+template <bool PD, int BEAM, bool REF, bool COUNT>
 static cudaError_t launch_shared_t(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
                                    const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
                                    const SimParams& p, const BeamDev& b, unsigned long long* bins,
-                                   cudaStream_t stream) {
+                                   unsigned long long* pair_counts, cudaStream_t stream) {
     if (chunk > 1024 || chunk % FOLD) return cudaErrorInvalidValue;
-    const size_t smem = 2 * (size_t)chunk * sizeof(float4);
+    size_t smem = 2 * (size_t)chunk * sizeof(float4);
     const int64_t chunks = (n + chunk - 1) / chunk;
-    if (p.wide_cta && L >= 768) {
-        // one 768-thread CTA per SM: all warps of an SM share one record chunk and
-        // the lookup-table planes it touches
-        auto k = project_shared_kernel<PD, BEAM, REF, 768>;
+    if (p.wide_cta && L >= 512) {
+        // large CTAs (one per SM with lookup-table planes): all warps of an SM
+        // share one record chunk and the lookup-table planes it touches, staged
+        // in shared memory (up to two planes: a chunk of <= 1024 records spans
+        // far less than a table cell radially in any dense phantom; records
+        // beyond them read the table through the cache).  1024 or 512 threads,
+        // whichever leaves fewer idle lanes in the last group of lines.
+        int lut_planes = 0;
+        if (BEAM == BEAM_LUT && !REF && p.lut_smem) {
+            const size_t plane_bytes = (size_t)b.nl * b.ne * sizeof(float4);
+            const size_t budget = 200 * 1024;
+            if (smem + plane_bytes <= budget) lut_planes = (budget - smem) / plane_bytes >= 2 ? 2 : 1;
+            smem += (size_t)lut_planes * plane_bytes;
+        }
+        const int64_t groups1024 = (L + 1023) / 1024, groups512 = (L + 511) / 512;
+        if (groups512 * 512 < groups1024 * 1024) {
+            auto k = project_shared_kernel<PD, BEAM, REF, 512, COUNT>;
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            k<<<(unsigned)chunks, 512, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
+                                                       p, b, lut_planes, pair_counts);
+            return cudaGetLastError();
+        }
+        auto k = project_shared_kernel<PD, BEAM, REF, 1024, COUNT>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k<<<(unsigned)chunks, 768, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
-                                                   p, b);
+        k<<<(unsigned)chunks, 1024, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
+                                                    p, b, lut_planes, pair_counts);
         return cudaGetLastError();
     }
-    auto k = project_shared_kernel<PD, BEAM, REF, 256>;
+    auto k = project_shared_kernel<PD, BEAM, REF, 256, COUNT>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int threads = L >= 256 ? 256 : ((L + 31) / 32) * 32;
     k<<<(unsigned)chunks, threads, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
-                                                   p, b);
+                                                   p, b, 0, pair_counts);
     return cudaGetLastError();
 }
 
 cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
                                   const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
                                   const SimParams& p, const BeamDev& b, unsigned long long* bins,
-                                  cudaStream_t stream) {
+                                  unsigned long long* pair_counts, cudaStream_t stream) {
     if (n <= 0 || L <= 0) return cudaSuccess;
     const bool pd = p.phase_delay != 0;
     const bool ref = p.mode == MODE_REFERENCE;
-#define BCSIM_SH(PDV, BM, R) \
-    launch_shared_t<PDV, BM, R>(records, plane, counts, n, chunk, lines, line_order, cones, L, p, b, bins, stream)
-    if (b.type == BEAM_GAUSSIAN) {
-        if (pd) return ref ? BCSIM_SH(true, BEAM_GAUSSIAN, true) : BCSIM_SH(true, BEAM_GAUSSIAN, false);
-        return ref ? BCSIM_SH(false, BEAM_GAUSSIAN, true) : BCSIM_SH(false, BEAM_GAUSSIAN, false);
+    if (pair_counts && ref) return cudaErrorInvalidValue;   // counting instruments the fp64-mode kernel only
+#define BCSIM_SH(PDV, BM, R, C) \
+    launch_shared_t<PDV, BM, R, C>(records, plane, counts, n, chunk, lines, line_order, cones, L, p, b, bins, pair_counts, stream)
+    if (pair_counts) {
+        if (b.type == BEAM_GAUSSIAN) return pd ? BCSIM_SH(true, BEAM_GAUSSIAN, false, true) : BCSIM_SH(false, BEAM_GAUSSIAN, false, true);
+        return pd ? BCSIM_SH(true, BEAM_LUT, false, true) : BCSIM_SH(false, BEAM_LUT, false, true);
     }
-    if (pd) return ref ? BCSIM_SH(true, BEAM_LUT, true) : BCSIM_SH(true, BEAM_LUT, false);
-    return ref ? BCSIM_SH(false, BEAM_LUT, true) : BCSIM_SH(false, BEAM_LUT, false);
+    if (b.type == BEAM_GAUSSIAN) {
+        if (pd) return ref ? BCSIM_SH(true, BEAM_GAUSSIAN, true, false) : BCSIM_SH(true, BEAM_GAUSSIAN, false, false);
+        return ref ? BCSIM_SH(false, BEAM_GAUSSIAN, true, false) : BCSIM_SH(false, BEAM_GAUSSIAN, false, false);
+    }
+    if (pd) return ref ? BCSIM_SH(true, BEAM_LUT, true, false) : BCSIM_SH(true, BEAM_LUT, false, false);
+    return ref ? BCSIM_SH(false, BEAM_LUT, true, false) : BCSIM_SH(false, BEAM_LUT, false, false);
 #undef BCSIM_SH
 }
 
