@@ -275,13 +275,14 @@ def run_gpu(args):
     # ---- one instrumented run (outside every timed region): the (record, line)
     # pairs the shared-origin kernel visits and those with a non-zero weight ----
     shared_path = "prep_sort_ms" in stage
-    visited = nonzero = None
+    visited = nonzero = idle_steps = None
     if shared_path:
         sim.set_parameter("count_pairs", "on")
         sim.simulate_lines_device(dev_out.data_ptr(), dev_out.numel())
         torch.cuda.synchronize()
         visited = int(sim.get_debug_data("evaluated_pairs")[0])
         nonzero = int(sim.get_debug_data("weighted_pairs")[0])
+        idle_steps = int(sim.get_debug_data("idle_walk_steps")[0])
         sim.set_parameter("count_pairs", "off")
 
     if rank != 0:
@@ -327,7 +328,8 @@ def run_gpu(args):
                      "frac": achieved_tflops / fp32_peak, "traffic": traffic,
                      "flops_per_unit": fpp, "units_per_launch": units,
                      "unit_counted": "visited (record, line) pairs" if shared_path else "(scatterer, line) pairs",
-                     "pairs": {"all": projections, "visited": visited, "nonzero_weight": nonzero},
+                     "pairs": {"all": projections, "visited": visited, "nonzero_weight": nonzero,
+                               "idle_warp_steps": idle_steps},
                      "all_pairs_convention": {"achieved": all_pairs_tflops, "frac": all_pairs_tflops / fp32_peak,
                                               "note": "flops_per_unit x N x L: counts the pairs of weight exactly 0 "
                                                       "that the slot masks skip, so it can exceed the peak"},

@@ -473,71 +473,117 @@ void Simulator::prepare_excitation_tables() {
     tables_valid_ = true;
 }
 
-// Kernel line order for the shared-origin kernel: lines sorted along a Morton
-// curve over their directions (projected on the plane normal to the mean
-// direction), so that every 32 consecutive lines point in nearby directions,
-// and the bounding cone of each such slot of 32.
+// Kernel line order for the shared-origin kernel: recursive bisection of the
+// lines by direction into slots of 32 -- each set is sorted along the major
+// principal axis of its directions (projected on the plane normal to their mean)
+// and cut at the multiple of 32 nearest its middle -- so that the 32 lines of a
+// slot point in a compact patch of directions (a 4 x 8 block of a regular
+// azimuth/elevation grid); then the frame spread of each slot about its line
+// nearest the slot's mean direction.
+namespace {
+struct Dir3 {
+    double x, y, z;
+};
+Dir3 unit_mean(const std::vector<LineGeom>& lines, const int* idx, int n) {
+    double m[3] = {0, 0, 0};
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++) m[k] += lines[idx[i]].d[k];
+    double mn = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    if (mn < 1e-12) return Dir3{0, 0, 1};
+    return Dir3{m[0] / mn, m[1] / mn, m[2] / mn};
+}
+void bisect_lines(const std::vector<LineGeom>& lines, int* idx, int n) {
+    if (n <= 32) return;
+    const Dir3 m = unit_mean(lines, idx, n);
+    // tangent basis (t1, t2) normal to m
+    double a[3] = {1, 0, 0};
+    if (std::fabs(m.x) > 0.9) { a[0] = 0; a[1] = 1; }
+    double t1[3] = {a[1] * m.z - a[2] * m.y, a[2] * m.x - a[0] * m.z, a[0] * m.y - a[1] * m.x};
+    const double n1 = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (double& v : t1) v /= n1;
+    const double t2[3] = {m.y * t1[2] - m.z * t1[1], m.z * t1[0] - m.x * t1[2], m.x * t1[1] - m.y * t1[0]};
+    std::vector<double> pu(n), pv(n);
+    double su = 0, sv = 0;
+    for (int i = 0; i < n; i++) {
+        const float* d = lines[idx[i]].d;
+        pu[i] = d[0] * t1[0] + d[1] * t1[1] + d[2] * t1[2];
+        pv[i] = d[0] * t2[0] + d[1] * t2[1] + d[2] * t2[2];
+        su += pu[i];
+        sv += pv[i];
+    }
+    su /= n;
+    sv /= n;
+    double cuu = 0, cuv = 0, cvv = 0;
+    for (int i = 0; i < n; i++) {
+        const double du = pu[i] - su, dv = pv[i] - sv;
+        cuu += du * du; cuv += du * dv; cvv += dv * dv;
+    }
+    // major axis of the 2 x 2 covariance
+    const double ang = 0.5 * std::atan2(2.0 * cuv, cuu - cvv);
+    const double ax = std::cos(ang), ay = std::sin(ang);
+    std::vector<std::pair<double, int>> key(n);
+    for (int i = 0; i < n; i++) key[i] = {(pu[i] - su) * ax + (pv[i] - sv) * ay, idx[i]};
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<double, int>& x, const std::pair<double, int>& y) { return x.first < y.first; });
+    for (int i = 0; i < n; i++) idx[i] = key[i].second;
+    int half = (int)std::lround(n / 64.0) * 32;
+    half = std::max(32, std::min(half, n - 32 > 32 ? n - 32 : 32));
+    bisect_lines(lines, idx, half);
+    bisect_lines(lines, idx + half, n - half);
+}
+}  // namespace
+
 static void order_lines(const std::vector<LineGeom>& lines, std::vector<int>& order, std::vector<SlotCone>& cones) {
     const int L = (int)lines.size();
     order.resize(L);
     std::iota(order.begin(), order.end(), 0);
-    double m[3] = {0, 0, 0};
-    for (const auto& g : lines)
-        for (int k = 0; k < 3; k++) m[k] += g.d[k];
-    double mn = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-    if (mn < 1e-12) { m[0] = 0; m[1] = 0; m[2] = 1; mn = 1; }
-    for (double& v : m) v /= mn;
-    // orthonormal e1, e2 perpendicular to m
-    double a[3] = {1, 0, 0};
-    if (std::fabs(m[0]) > 0.9) { a[0] = 0; a[1] = 1; }
-    double e1[3] = {a[1] * m[2] - a[2] * m[1], a[2] * m[0] - a[0] * m[2], a[0] * m[1] - a[1] * m[0]};
-    const double n1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-    for (double& v : e1) v /= n1;
-    const double e2[3] = {m[1] * e1[2] - m[2] * e1[1], m[2] * e1[0] - m[0] * e1[2], m[0] * e1[1] - m[1] * e1[0]};
-    std::vector<double> u(L), v(L);
-    double umin = 1e300, umax = -1e300, vmin = 1e300, vmax = -1e300;
-    for (int i = 0; i < L; i++) {
-        const float* d = lines[i].d;
-        u[i] = d[0] * e1[0] + d[1] * e1[1] + d[2] * e1[2];
-        v[i] = d[0] * e2[0] + d[1] * e2[1] + d[2] * e2[2];
-        umin = std::min(umin, u[i]); umax = std::max(umax, u[i]);
-        vmin = std::min(vmin, v[i]); vmax = std::max(vmax, v[i]);
-    }
-    const double span = std::max(umax - umin, vmax - vmin) + 1e-12;
-    std::vector<uint32_t> key(L);
-    for (int i = 0; i < L; i++) {
-        const uint32_t qu = (uint32_t)std::min(65535.0, (u[i] - umin) / span * 65535.0);
-        const uint32_t qv = (uint32_t)std::min(65535.0, (v[i] - vmin) / span * 65535.0);
-        uint32_t k = 0;
-        for (int bit = 0; bit < 16; bit++) k |= ((qu >> bit) & 1u) << (2 * bit) | ((qv >> bit) & 1u) << (2 * bit + 1);
-        key[i] = k;
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return key[x] < key[y]; });
+    bisect_lines(lines, order.data(), L);
     const int slots = (L + 31) / 32;
-    cones.assign(slots, SlotCone{0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2});
+    cones.assign(slots, SlotCone{0, 0, 0, 0, 0, 0, 0, 0, 0, 2, 2, 2, 2, 2});
     for (int s = 0; s < slots; s++) {
         const int lo = s * 32, hi = std::min(L, lo + 32);
-        const LineGeom& ref = lines[order[(lo + hi) / 2]];
-        double du = 0, dv = 0, dd = 0;
+        const Dir3 m = unit_mean(lines, order.data() + lo, hi - lo);
+        int best = order[lo];
+        double best_dot = -2.0;
+        for (int i = lo; i < hi; i++) {
+            const float* d = lines[order[i]].d;
+            const double dot = d[0] * m.x + d[1] * m.y + d[2] * m.z;
+            if (dot > best_dot) { best_dot = dot; best = order[i]; }
+        }
+        const LineGeom& ref = lines[best];
+        double upar = 0, uperp = 0, vpar = 0, vperp = 0, dd = 0;
         for (int i = lo; i < hi; i++) {
             const LineGeom& g = lines[order[i]];
-            double a = 0, b = 0, c = 0;
+            double dl[3], de[3], pl = 0, pe = 0, c = 0;
             for (int k = 0; k < 3; k++) {
-                a += ((double)g.l[k] - ref.l[k]) * ((double)g.l[k] - ref.l[k]);
-                b += ((double)g.e[k] - ref.e[k]) * ((double)g.e[k] - ref.e[k]);
+                dl[k] = (double)g.l[k] - ref.l[k];
+                de[k] = (double)g.e[k] - ref.e[k];
+                pl += dl[k] * ref.d[k];
+                pe += de[k] * ref.d[k];
                 c += ((double)g.d[k] - ref.d[k]) * ((double)g.d[k] - ref.d[k]);
             }
-            du = std::max(du, std::sqrt(a));
-            dv = std::max(dv, std::sqrt(b));
+            double ql = 0, qe = 0;
+            for (int k = 0; k < 3; k++) {
+                const double xl = dl[k] - pl * ref.d[k], xe = de[k] - pe * ref.d[k];
+                ql += xl * xl;
+                qe += xe * xe;
+            }
+            upar = std::max(upar, std::fabs(pl));
+            uperp = std::max(uperp, std::sqrt(ql));
+            vpar = std::max(vpar, std::fabs(pe));
+            vperp = std::max(vperp, std::sqrt(qe));
             dd = std::max(dd, std::sqrt(c));
         }
         SlotCone cone;
         cone.lx = ref.l[0]; cone.ly = ref.l[1]; cone.lz = ref.l[2];
         cone.ex = ref.e[0]; cone.ey = ref.e[1]; cone.ez = ref.e[2];
         cone.rx = ref.d[0]; cone.ry = ref.d[1]; cone.rz = ref.d[2];
-        // margin for the float rounding of the test's dot products
-        cone.du = (float)(du * 1.0001 + 2e-6);
-        cone.dv = (float)(dv * 1.0001 + 2e-6);
+        // margins for the float rounding of the test's products (the frames are
+        // unit vectors to float precision, so their own rounding is covered too)
+        cone.du_par = (float)(upar * 1.0001 + 2e-6);
+        cone.du_perp = (float)(uperp * 1.0001 + 2e-6);
+        cone.dv_par = (float)(vpar * 1.0001 + 2e-6);
+        cone.dv_perp = (float)(vperp * 1.0001 + 2e-6);
         cone.dd = (float)(dd * 1.0001 + 2e-6);
         cones[s] = cone;
     }
@@ -575,7 +621,13 @@ double Simulator::fixed_point_bound() const {
 
 // Packed LUT: at (r, l, e) the corners (c[r][l][e], c[r][l][e+1], c[r+1][l][e],
 // c[r+1][l][e+1]), zero past the last sample.
-static std::vector<float4> pack_lut(const std::vector<float>& c, int nr, int nl, int ne) {
+// Packed table: at (r, l, e) the corners needed by one trilinear lookup with
+// radial index r, (c[r][l][e], c[r][l][e+1], c[r+1][l][e], c[r+1][l][e+1]).
+// With radial_diff the last two hold the radial differences
+// c[r+1][.][.] - c[r][.][.] instead (the float subtraction the fp64-mode
+// kernels would otherwise do per lookup: same value, one instruction less per
+// radial interpolation); the reference-arithmetic kernels take the corners.
+static std::vector<float4> pack_lut(const std::vector<float>& c, int nr, int nl, int ne, bool radial_diff) {
     std::vector<float4> p((size_t)nr * nl * ne);
     auto at = [&](int r, int l, int e) -> float {
         if (r >= nr || l >= nl || e >= ne) return 0.0f;
@@ -583,8 +635,10 @@ static std::vector<float4> pack_lut(const std::vector<float>& c, int nr, int nl,
     };
     for (int r = 0; r < nr; r++)
         for (int l = 0; l < nl; l++)
-            for (int e = 0; e < ne; e++)
-                p[((size_t)r * nl + l) * ne + e] = make_float4(at(r, l, e), at(r, l, e + 1), at(r + 1, l, e), at(r + 1, l, e + 1));
+            for (int e = 0; e < ne; e++) {
+                const float c0 = at(r, l, e), c1 = at(r, l, e + 1), c2 = at(r + 1, l, e), c3 = at(r + 1, l, e + 1);
+                p[((size_t)r * nl + l) * ne + e] = radial_diff ? make_float4(c0, c1, c2 - c0, c3 - c1) : make_float4(c0, c1, c2, c3);
+            }
     return p;
 }
 
@@ -648,12 +702,13 @@ void Simulator::prepare() {
         b.two_sl2 = 2 * sigma_l_ * sigma_l_;
         b.two_se2 = 2 * sigma_e_ * sigma_e_;
     } else {
-        if (!lut_uploaded_) {
-            const auto packed = pack_lut(lut_, lut_nr_, lut_nl_, lut_ne_);
+        if (!lut_uploaded_ || lut_packed_mode_ != mode_) {
+            const auto packed = pack_lut(lut_, lut_nr_, lut_nl_, lut_ne_, mode_ == MODE_FP64);
             lut4_.reserve(packed.size() * sizeof(float4));
             BCSIM_CUDA(cudaMemcpyAsync(lut4_.get(), packed.data(), packed.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
             BCSIM_CUDA(cudaStreamSynchronize(st));
             lut_uploaded_ = true;
+            lut_packed_mode_ = mode_;
         }
         b.lut4 = lut4_.as<float4>();
         b.nr = lut_nr_; b.nl = lut_nl_; b.ne = lut_ne_;
@@ -824,7 +879,7 @@ void Simulator::prepare() {
     P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
     bins_.reserve(P.bins_bytes);
     counts_.reserve(4 * sizeof(int));
-    pair_counts_.reserve(2 * sizeof(unsigned long long));
+    pair_counts_.reserve(3 * sizeof(unsigned long long));
     out_.reserve((size_t)L * nd_ * sizeof(float2));
     P.spline_off.assign(splines_.size(), -1);
     if (P.n_shared > 0) {
@@ -939,7 +994,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
         unsigned long long* pair_counts = nullptr;
         if (count_pairs_ && p.mode == MODE_FP64) {
             pair_counts = pair_counts_.as<unsigned long long>();
-            BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 2 * sizeof(unsigned long long), st));
+            BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 3 * sizeof(unsigned long long), st));
         }
         ++launches;
         BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
@@ -1008,11 +1063,12 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     const cudaStream_t st = stream_;
     enqueue(st, dev_out, store_details_);
     if (count_pairs_ && plan_.n_shared > 0 && mode_ == MODE_FP64) {
-        unsigned long long c[2] = {0, 0};
+        unsigned long long c[3] = {0, 0, 0};
         BCSIM_CUDA(cudaMemcpyAsync(c, pair_counts_.get(), sizeof c, cudaMemcpyDeviceToHost, st));
         BCSIM_CUDA(cudaStreamSynchronize(st));
         debug_["evaluated_pairs"] = {(double)c[0]};
         debug_["weighted_pairs"] = {(double)c[1]};
+        debug_["idle_walk_steps"] = {(double)c[2]};
     }
     if (host_out) {
         EventTimer timer(store_details_, st);

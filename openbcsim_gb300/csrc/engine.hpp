@@ -195,6 +195,7 @@ private:
     double lut_absmax_ = 0.0;
     DeviceBuffer lut4_;
     bool lut_uploaded_ = false;
+    int lut_packed_mode_ = -1;   // precision mode the uploaded packing is for (pack_lut)
 
     // all fixed datasets, appended into one float4 [n] array (x, y, z, a)
     DeviceBuffer fixed_xyza_;

@@ -26,7 +26,7 @@ struct BeamDev {
     float gl, ge;
     // Gaussian, reference mode: w = expf(-(l*l/two_sl2 + e*e/two_se2)) (BeamProfile.cpp:49-56)
     float two_sl2, two_se2;
-    // Lookup table: packed corners, see pack_lut() in engine.cpp
+    // Lookup table: packed corners (fp64 mode: with radial differences), see pack_lut() in engine.cpp
     const float4* lut4;
     int nr, nl, ne;
     float rf, lf, ef;          // first sample positions
@@ -57,12 +57,16 @@ struct SimParams {
 };
 
 // Frame spread of a slot of 32 lines (consecutive in the kernel's line order):
-// a reference frame (lateral l, elevational e, radial r) and the largest
-// difference between any line's frame vector and it (du, dv, dd), so that for a
-// scatterer at distance rho every line's coordinate lies within rho * d of the
-// reference coordinate.
+// a reference frame (lateral l, elevational e, radial r) and, for the
+// differences dl = l_k - l and de = e_k - e of every line k of the slot, their
+// largest component along r (du_par, dv_par) and largest part normal to r
+// (du_perp, dv_perp), and the largest |r_k - r| (dd).  For a scatterer at
+// offset A = t r + A_perp from the origin every line's lateral coordinate then
+// lies within |t| du_par + |A_perp| du_perp of A.l (elevational alike), and
+// every line's radial coordinate within |A| dd of A.r.
 struct SlotCone {
-    float lx, ly, lz, ex, ey, ez, rx, ry, rz, du, dv, dd;
+    float lx, ly, lz, ex, ey, ez, rx, ry, rz;
+    float du_par, du_perp, dv_par, dv_perp, dd;
 };
 
 // A tile of lines for the per-pair projection kernel: `count` lines taken from
@@ -121,7 +125,8 @@ cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts
 // origin); `chunk` records per CTA, lines taken in the order line_order[] with
 // slot cones[] per 32 of them.  pair_counts (fp64 mode only; normally null):
 // when set, a counting variant adds the (record, line) pairs it visits to
-// pair_counts[0] and those with a non-zero beam weight to pair_counts[1].
+// pair_counts[0], those with a non-zero beam weight to pair_counts[1] and the
+// warp walk steps in which no lane had a non-zero weight to pair_counts[2].
 cudaError_t launch_project_shared(const float4* records, int64_t plane, const int* counts, int64_t n, int chunk,
                                   const LineGeom* lines, const int* line_order, const SlotCone* cones,
                                   int num_lines, const SimParams& p, const BeamDev& b, unsigned long long* bins,

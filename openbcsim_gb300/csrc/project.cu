@@ -61,13 +61,14 @@ __device__ __forceinline__ float lut_weight_packed(const BeamDev& b, int r0, flo
     const float fl = tl < 0.0f ? 0.0f : tl - (float)l0;
     const float fe = te < 0.0f ? 0.0f : te - (float)e0;
     const int base = (r0 * b.nl + l0) * b.ne + e0;
-    const float4 P = __ldg(b.lut4 + base);            // (r0,l0,e0) (r0,l0,e1) (r1,l0,e0) (r1,l0,e1)
-    const float4 Q = __ldg(b.lut4 + base + b.ne);     // same at l1
+    // (r0,l0,e0) (r0,l0,e1) and the radial differences to r1 at both, then the same at l1
+    const float4 P = __ldg(b.lut4 + base);
+    const float4 Q = __ldg(b.lut4 + base + b.ne);
     // radial, then lateral, then elevational interpolation (BeamProfile.cpp:116-127)
-    const float c00 = __fmaf_rn(fr, P.z - P.x, P.x);
-    const float c01 = __fmaf_rn(fr, P.w - P.y, P.y);
-    const float c10 = __fmaf_rn(fr, Q.z - Q.x, Q.x);
-    const float c11 = __fmaf_rn(fr, Q.w - Q.y, Q.y);
+    const float c00 = __fmaf_rn(fr, P.z, P.x);
+    const float c01 = __fmaf_rn(fr, P.w, P.y);
+    const float c10 = __fmaf_rn(fr, Q.z, Q.x);
+    const float c11 = __fmaf_rn(fr, Q.w, Q.y);
     const float c0 = __fmaf_rn(fl, c10 - c00, c00);
     const float c1 = __fmaf_rn(fl, c11 - c01, c01);
     return __fmaf_rn(fe, c1 - c0, c0);
@@ -361,9 +362,10 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
 //   A. mask: each lane tests one record against the warp's "slot box": the
 //      lateral/elevational ranges outside which every line of the slot has
 //      weight exactly 0 (the lookup table's extent, or where exp2 underflows),
-//      widened by the spread of the slot's line frames times the record's
-//      distance bound.  32 records per instruction; one ballot word per 32
-//      records, word w kept by lane w.
+//      widened by the spread of the slot's line frames (along the slot's
+//      radial direction times the record's radial coordinate, normal to it times
+//      the record's distance from the axis).  32 records per instruction; one
+//      ballot word per 32 records, word w kept by lane w.
 //   B. walk: only the records whose bit is set, in bin order.  A line's
 //      contributions to one bin are summed in FP32, folded into an int64 total
 //      at absolute record indices k*FOLD, and written when the bin changes: a
@@ -446,7 +448,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             const float lx = __ldg(&c->lx), ly = __ldg(&c->ly), lz = __ldg(&c->lz);
             const float ex = __ldg(&c->ex), ey = __ldg(&c->ey), ez = __ldg(&c->ez);
             const float rx = __ldg(&c->rx), ry = __ldg(&c->ry), rz = __ldg(&c->rz);
-            const float du = __ldg(&c->du), dv = __ldg(&c->dv), dd = __ldg(&c->dd);
+            const float du_par = __ldg(&c->du_par), du_perp = __ldg(&c->du_perp);
+            const float dv_par = __ldg(&c->dv_par), dv_perp = __ldg(&c->dv_perp), dd = __ldg(&c->dd);
             mask = 0;
             for (int w = 0; w < nwords; w++) {
                 const int r = (w << 5) + lane;
@@ -459,7 +462,12 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
                     const float v = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
                     const float dt = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
-                    const float su = rho * du, sv = rho * dv;
+                    // |A_perp| = |A x r| (no cancellation for A along r), rounded up
+                    const float cx = fmaf(A.y, rz, -A.z * ry), cy = fmaf(A.z, rx, -A.x * rz);
+                    const float cz = fmaf(A.x, ry, -A.y * rx);
+                    const float ap = __fsqrt_ru(fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
+                    const float adt = fabsf(dt);
+                    const float su = fmaf(adt, du_par, ap * du_perp), sv = fmaf(adt, dv_par, ap * dv_perp);
                     pass = (u + su > p.cull_l_lo) && (u - su < p.cull_l_hi) && (v + sv > p.cull_e_lo) &&
                            (v - sv < p.cull_e_hi) && (dt + rho * dd >= 0.0f);
                 }
@@ -469,7 +477,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         }
 
         // ---- phase B: walk the selected records in bin order ----
-        unsigned walked = 0, weighted = 0;   // COUNT: pairs visited, pairs with a non-zero weight
+        // COUNT: pairs visited, pairs with a non-zero weight, walk steps in which
+        // no lane of the warp had a non-zero weight
+        unsigned walked = 0, weighted = 0, idle_steps = 0;
         int cur = first_bin;
         long long tr = 0, ti = 0;
         float ar = 0.0f, ai = 0.0f;
@@ -557,11 +567,12 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                                     Q = __ldg(b.lut4 + base + b.ne);
                                 }
                                 const float fr = B.y;
-                                // radial, lateral, elevational (BeamProfile.cpp:116-127)
-                                const float c00 = fmaf(fr, P.z - P.x, P.x);
-                                const float c01 = fmaf(fr, P.w - P.y, P.y);
-                                const float c10 = fmaf(fr, Q.z - Q.x, Q.x);
-                                const float c11 = fmaf(fr, Q.w - Q.y, Q.y);
+                                // radial (the table holds the radial differences),
+                                // lateral, elevational (BeamProfile.cpp:116-127)
+                                const float c00 = fmaf(fr, P.z, P.x);
+                                const float c01 = fmaf(fr, P.w, P.y);
+                                const float c10 = fmaf(fr, Q.z, Q.x);
+                                const float c11 = fmaf(fr, Q.w, Q.y);
                                 const float c0 = fmaf(fl, c10 - c00, c00);
                                 const float c1 = fmaf(fl, c11 - c01, c01);
                                 w8 = fmaf(fe, c1 - c0, c0);
@@ -573,6 +584,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     if (COUNT) {
                         walked += active ? 1u : 0u;
                         weighted += (active && w8 != 0.0f) ? 1u : 0u;
+                        idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
                     }
                 }
             }
@@ -587,6 +599,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             if (lane == 0) {
                 atomicAdd(pair_counts, (unsigned long long)walked);
                 atomicAdd(pair_counts + 1, (unsigned long long)weighted);
+                atomicAdd(pair_counts + 2, (unsigned long long)idle_steps);
             }
         }
         if (active) {
