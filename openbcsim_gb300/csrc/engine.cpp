@@ -724,6 +724,7 @@ void Simulator::prepare() {
             b.de = (double)((lut_ext_[5] - lut_ext_[4]) / (lut_ne_ - 1));
         }
         b.inv_dr = (float)(1.0 / b.dr);
+        b.inv_dr_lo = (float)(1.0 / b.dr - (double)b.inv_dr);
         b.inv_dl = (float)(1.0 / b.dl);
         b.inv_de = (float)(1.0 / b.de);
     }

@@ -31,6 +31,7 @@ struct BeamDev {
     int nr, nl, ne;
     float rf, lf, ef;          // first sample positions
     float inv_dr, inv_dl, inv_de;  // 1 / spacing (fp64 mode, per-pair coordinates)
+    float inv_dr_lo;           // 1/dr - inv_dr: 1/dr as a float pair (fp64-mode record prep)
     double dr, dl, de;         // spacing as the mode defines it (double)
 };
 

@@ -115,26 +115,98 @@ struct PrepOut {
     float4 A, B;
 };
 
-// dx,dy,dz: the scatterer relative to the origin in double (fp64 mode) and as
-// the reference's float subtraction (reference mode); a: amplitude.
-// spline selects the spline loop's index expression r*2/(c*dt), dt = 1/fs
-// (CpuAlgorithm.cpp:161-162), over the fixed loop's r*2*fs/c (:75).
-__device__ __forceinline__ PrepOut prep_one(double dx, double dy, double dz, float fdx, float fdy, float fdz,
-                                            float a, const SimParams& p, const BeamDev& b, bool spline) {
+// fp64 mode.  (dx, dy, dz): the scatterer relative to the origin in double
+// and (px, py, pz) the same as float pairs; a: amplitude.  The distance and the
+// time of flight t = |d| 2 fs / c are evaluated in float-pair arithmetic (about
+// 2^-44 relative error); the bin index floor(t + 1/2) is taken from it unless t
+// lies within 2^-36 t of a rounding boundary, where the FP64 oracle's own
+// expression decides (fixed loop r*2*fs/c, CpuAlgorithm.cpp:75; spline loop
+// r*2/(c*dt), :161-162) -- so the index is the oracle's for every scatterer.
+// The sub-sample phase (CpuAlgorithm.cpp:85-92, |argument| <= pi fd/fs) and the
+// lookup-table radial coordinate are FP32 / float-pair.
+__device__ __forceinline__ PrepOut prep_fp64(double dx, double dy, double dz, df px, df py, df pz, float fdx,
+                                             float fdy, float fdz, float a, const SimParams& p, const BeamDev& b,
+                                             bool spline) {
     PrepOut o;
-    double rho, t;
-    if (p.mode == MODE_FP64) {
-        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-        rho = __dsqrt_rn(r2);
+    // |d|^2 = sum hi^2 (exact products) + 2 hi lo, then its square root
+    const df x2 = two_prod(px.hi, px.hi), y2 = two_prod(py.hi, py.hi), z2 = two_prod(pz.hi, pz.hi);
+    const df s1 = two_sum(x2.hi, y2.hi);
+    const df s2 = two_sum(s1.hi, z2.hi);
+    float lo = s1.lo + s2.lo + x2.lo + y2.lo + z2.lo;
+    lo = fmaf(2.0f * px.hi, px.lo, lo);
+    lo = fmaf(2.0f * py.hi, py.lo, lo);
+    lo = fmaf(2.0f * pz.hi, pz.lo, lo);
+    const df rho = df_sqrt(fast_two_sum(s2.hi, lo));
+    const df t = df_mul(rho, df_make(p.k_hi, p.k_lo));
+    uint32_t key;
+    int idx = 0;
+    float delay = 0.0f;   // idx - t, samples
+    if (!(t.hi < (float)p.ns + 1.0f)) {
+        key = (uint32_t)p.ns + 1u;                // beyond the line end for every line (or NaN)
     } else {
-        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), __fmul_rn(fdz, fdz));
-        rho = (double)__fsqrt_rn(r2);
+        const float f = floorf(t.hi);
+        const float g = (t.hi - f - 0.5f) + t.lo;   // t + 1/2 - (f + 1); t.hi - f and its difference with 1/2 are exact
+        if (fabsf(g) <= fmaf(fabsf(t.hi), 0x1p-36f, 0x1p-60f)) {
+            double t64;
+            const double rho64 = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+            if (!spline) t64 = __ddiv_rn(__dmul_rn(__dmul_rn(rho64, 2.0), p.fs_d), p.c_d);
+            else t64 = __ddiv_rn(__dmul_rn(rho64, 2.0), __dmul_rn(p.c_d, __ddiv_rn(1.0, p.fs_d)));
+            const double fidx = floor(t64 + 0.5);
+            idx = (int)fidx;
+            delay = (float)(fidx - t64);
+            if (!(fidx < (double)p.ns)) key = (uint32_t)p.ns + 1u;
+            else if (t64 <= 0.5) key = (uint32_t)p.ns;
+            else key = (uint32_t)idx;
+        } else {
+            idx = (int)f + (g >= 0.0f ? 1 : 0);
+            delay = ((float)idx - t.hi) - t.lo;
+            if (idx >= p.ns) key = (uint32_t)p.ns + 1u;
+            else if ((t.hi - 0.5f) + t.lo <= 0.0f) key = (uint32_t)p.ns;   // near origin: a line behind may still hit bin 0
+            else key = (uint32_t)idx;
+        }
     }
+    float Ar = a, Ai = 0.0f;
+    if (p.phase_delay && key < (uint32_t)p.ns) {
+        float sn, cs;
+        sincosf(p.two_pi_fd_over_fs * delay, &sn, &cs);
+        Ar = a * cs;
+        Ai = a * sn;
+    }
+    int r0 = 0;
+    float fr = 0.0f;
+    if (b.type == BEAM_LUT && key < (uint32_t)p.ns) {
+        // (|d| - r_first) / dr as a pair; valid for -1 < tr < nr-1 (BeamProfile.cpp:94-103)
+        df q = two_sum(rho.hi, -b.rf);
+        q = fast_two_sum(q.hi, q.lo + rho.lo);
+        const df tr = df_mul(q, df_make(b.inv_dr, b.inv_dr_lo));
+        if (!((tr.hi + 1.0f) + tr.lo > 0.0f && (tr.hi - (float)(b.nr - 1)) + tr.lo < 0.0f)) {
+            key = (uint32_t)p.ns + 1u;            // radial coordinate outside the table: weight 0
+        } else if (tr.hi + tr.lo > 0.0f) {
+            float f = floorf(tr.hi);
+            float rem = tr.hi - f;
+            if (rem + tr.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
+            r0 = (int)f;
+            fr = rem + tr.lo;
+        }                                          // -1 < tr <= 0: index 0, fraction dropped
+    }
+    o.key = key;
+    o.A = make_float4(fdx, fdy, fdz, Ar);
+    o.B = make_float4(Ai, fr, __int_as_float(r0), __int_as_float(idx));
+    return o;
+}
+
+// Reference mode: the reference's float distance and its double index
+// expression (fixed r*2*fs/c, CpuAlgorithm.cpp:75; spline r*2/(c*dt) with
+// dt = float(1/fs), :161-162), float phase from a double delay (:85-92), and
+// the lookup-table coordinate of BeamProfile.cpp:94-103.
+__device__ __forceinline__ PrepOut prep_ref(float fdx, float fdy, float fdz, float a, const SimParams& p,
+                                            const BeamDev& b, bool spline) {
+    PrepOut o;
+    const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(fdx, fdx), __fmul_rn(fdy, fdy)), __fmul_rn(fdz, fdz));
+    const double rho = (double)__fsqrt_rn(r2);
+    double t;
     if (!spline) {
-        // t = r * 2.0 * fs / c, evaluated left to right as CpuAlgorithm.cpp:75
         t = __ddiv_rn(__dmul_rn(__dmul_rn(rho, 2.0), p.fs_d), p.c_d);
-    } else if (p.mode == MODE_FP64) {
-        t = __ddiv_rn(__dmul_rn(rho, 2.0), __dmul_rn(p.c_d, __ddiv_rn(1.0, p.fs_d)));
     } else {
         const float dt = (float)(1.0 / p.fs_d);
         t = __ddiv_rn(__dmul_rn(rho, 2.0), (double)__fmul_rn(p.c, dt));
@@ -151,28 +223,17 @@ __device__ __forceinline__ PrepOut prep_one(double dx, double dy, double dz, flo
     const int idx = (int)fidx;
     float Ar = a, Ai = 0.0f;
     if (p.phase_delay && key < (uint32_t)p.ns) {
-        if (p.mode == MODE_FP64) {
-            const double delay = ((double)idx - t) / p.fs_d;
-            const double ph = TWO_PI_LITERAL * p.fd_d * delay;
-            double s, c;
-            sincos(ph, &s, &c);
-            Ar = (float)((double)a * c);
-            Ai = (float)((double)a * s);
-        } else {
-            const float ss_delay = (float)(((double)idx - t) / p.fs_d);
-            const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
-            float s, c;
-            sincosf(ph, &s, &c);
-            Ar = __fmul_rn(a, c);
-            Ai = __fmul_rn(a, s);
-        }
+        const float ss_delay = (float)(((double)idx - t) / p.fs_d);
+        const float ph = (float)(TWO_PI_LITERAL * p.fd_d * (double)ss_delay);
+        float sn, cs;
+        sincosf(ph, &sn, &cs);
+        Ar = __fmul_rn(a, cs);
+        Ai = __fmul_rn(a, sn);
     }
     int r0 = 0;
     float fr = 0.0f;
     if (b.type == BEAM_LUT && key < (uint32_t)p.ns) {
-        double tr;
-        if (p.mode == MODE_FP64) tr = (rho - (double)b.rf) / b.dr;
-        else tr = (double)__fsub_rn((float)rho, b.rf) / b.dr;
+        const double tr = (double)__fsub_rn((float)rho, b.rf) / b.dr;
         if (!(tr > -1.0 && tr < (double)(b.nr - 1))) {
             key = (uint32_t)p.ns + 1u;           // radial coordinate outside the table: weight 0
         } else {
@@ -193,9 +254,15 @@ __global__ void prep_shared_kernel(const float4* __restrict__ xyza, int64_t n, i
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float4 q = __ldg(xyza + i);
-    const double dx = __dsub_rn((double)q.x, ox), dy = __dsub_rn((double)q.y, oy), dz = __dsub_rn((double)q.z, oz);
-    const float fdx = __fsub_rn(q.x, ofx), fdy = __fsub_rn(q.y, ofy), fdz = __fsub_rn(q.z, ofz);
-    const PrepOut o = prep_one(dx, dy, dz, fdx, fdy, fdz, q.w, p, b, false);
+    PrepOut o;
+    if (p.mode == MODE_FP64) {
+        // q - origin: exact as float pairs and in double
+        const df px = two_sum(q.x, -ofx), py = two_sum(q.y, -ofy), pz = two_sum(q.z, -ofz);
+        const double dx = __dsub_rn((double)q.x, ox), dy = __dsub_rn((double)q.y, oy), dz = __dsub_rn((double)q.z, oz);
+        o = prep_fp64(dx, dy, dz, px, py, pz, px.hi, py.hi, pz.hi, q.w, p, b, false);
+    } else {
+        o = prep_ref(__fsub_rn(q.x, ofx), __fsub_rn(q.y, ofy), __fsub_rn(q.z, ofz), q.w, p, b, false);
+    }
     keys[off + i] = o.key;
     vals[off + i] = (uint32_t)(off + i);
     recA[off + i] = o.A;
@@ -227,16 +294,18 @@ __global__ void prep_shared_spline_kernel(const float4* __restrict__ cps, const 
             fz = __fadd_rn(fz, __fmul_rn(c.z, bf[k]));
         }
     }
-    double dx, dy, dz;
-    float fdx, fdy, fdz;
+    PrepOut o;
     if (p.mode == MODE_FP64) {
-        dx = __dsub_rn(px, ox); dy = __dsub_rn(py, oy); dz = __dsub_rn(pz, oz);
-        fdx = (float)dx; fdy = (float)dy; fdz = (float)dz;
+        const double dx = __dsub_rn(px, ox), dy = __dsub_rn(py, oy), dz = __dsub_rn(pz, oz);
+        // the double offsets as float pairs (48 of their 53 bits)
+        const float hx = __double2float_rn(dx), hy = __double2float_rn(dy), hz = __double2float_rn(dz);
+        const df qx = fast_two_sum(hx, __double2float_rn(__dsub_rn(dx, (double)hx)));
+        const df qy = fast_two_sum(hy, __double2float_rn(__dsub_rn(dy, (double)hy)));
+        const df qz = fast_two_sum(hz, __double2float_rn(__dsub_rn(dz, (double)hz)));
+        o = prep_fp64(dx, dy, dz, qx, qy, qz, hx, hy, hz, __ldg(amps + i), p, b, true);
     } else {
-        fdx = __fsub_rn(fx, ofx); fdy = __fsub_rn(fy, ofy); fdz = __fsub_rn(fz, ofz);
-        dx = fdx; dy = fdy; dz = fdz;
+        o = prep_ref(__fsub_rn(fx, ofx), __fsub_rn(fy, ofy), __fsub_rn(fz, ofz), __ldg(amps + i), p, b, true);
     }
-    const PrepOut o = prep_one(dx, dy, dz, fdx, fdy, fdz, __ldg(amps + i), p, b, true);
     keys[off + i] = o.key;
     vals[off + i] = (uint32_t)(off + i);
     recA[off + i] = o.A;
@@ -390,8 +459,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     const int lane = tid & 31;
     float4* smA = sm;
     float4* smB = sm + chunk;
-    float4* smL = sm + 2 * chunk;   // lut_planes radial planes of the packed table
+    // lut_planes radial planes of the packed table, rows padded to an odd number
+    // of float4 so that the lanes' corner gathers spread over the banks
+    float4* smL = sm + 2 * chunk;
     const int lut_plane_size = b.nl * b.ne;
+    const int lut_row = b.ne | 1, lut_splane = b.nl * lut_row;
 
     if (tid == 0) {
         mbar_init(&bar, 1);
@@ -411,11 +483,18 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     const int lut_base = s_lut_base, lut_staged = s_lut_planes;
     if (tid == 0) {
         const unsigned bytes = (unsigned)cnt * sizeof(float4);
-        const unsigned lut_bytes = (unsigned)lut_staged * (unsigned)lut_plane_size * (unsigned)sizeof(float4);
-        mbar_expect_tx(&bar, 2 * bytes + lut_bytes);
+        mbar_expect_tx(&bar, 2 * bytes);
         bulk_load(smA, records + start, bytes, &bar);
         bulk_load(smB, records + plane + start, bytes, &bar);
-        if (lut_bytes) bulk_load(smL, b.lut4 + (int64_t)lut_base * lut_plane_size, lut_bytes, &bar);
+    }
+    if (lut_staged > 0) {   // (BEAM == BEAM_LUT only) while the records arrive
+        const float4* src = b.lut4 + (int64_t)lut_base * lut_plane_size;
+        for (int k = tid; k < lut_staged * lut_plane_size; k += blockDim.x) {
+            const int pl = k / lut_plane_size, rem = k - pl * lut_plane_size;
+            const int l = rem / b.ne, e = rem - l * b.ne;
+            smL[pl * lut_splane + l * lut_row + e] = __ldg(src + k);
+        }
+        __syncthreads();
     }
     if (!mbar_wait(&bar, 0, 1u << 26)) {
         g_bcsim_error_flag = 1;
@@ -555,14 +634,13 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                                 const float fl = uc - (tu - 8388608.0f);
                                 const float fe = vc - (tv - 8388608.0f);
                                 const int r0 = __float_as_int(B.z);
-                                const int off = l0 * b.ne + e0;
                                 float4 P, Q;
                                 if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
-                                    const float4* pl = smL + (r0 - lut_base) * lut_plane_size + off;
+                                    const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
                                     P = pl[0];
-                                    Q = pl[b.ne];
+                                    Q = pl[lut_row];
                                 } else {
-                                    const int base = r0 * lut_plane_size + off;
+                                    const int base = r0 * lut_plane_size + l0 * b.ne + e0;
                                     P = __ldg(b.lut4 + base);
                                     Q = __ldg(b.lut4 + base + b.ne);
                                 }
@@ -937,7 +1015,7 @@ static cudaError_t launch_shared_t(const float4* records, int64_t plane, const i
         // whichever leaves fewer idle lanes in the last group of lines.
         int lut_planes = 0;
         if (BEAM == BEAM_LUT && !REF && p.lut_smem) {
-            const size_t plane_bytes = (size_t)b.nl * b.ne * sizeof(float4);
+            const size_t plane_bytes = (size_t)b.nl * (b.ne | 1) * sizeof(float4);
             const size_t budget = 200 * 1024;
             if (smem + plane_bytes <= budget) lut_planes = (budget - smem) / plane_bytes >= 2 ? 2 : 1;
             smem += (size_t)lut_planes * plane_bytes;
