@@ -25,6 +25,7 @@
 // conflicts); sub-rows are padded to 4 mod 16 elements so that the staging
 // stores, which cover all four sub-rows, do not conflict either.  The taps are
 // stored phase-major on the host, zero-padded to a multiple of 4 per phase.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "kernels.hpp"
@@ -70,9 +71,13 @@ __global__ void __launch_bounds__(256)
     const long long mmask = (long long)M - 1;
     const int stride = PD ? 2 : 1;
     const long long* lb = (const long long*)bins + (int64_t)line * ns * stride;
+    // the last block of a line may hold fewer than per_cta outputs: stage only
+    // the columns its threads read
+    const int valid = min(per_cta, nd - m0);
+    const int cols_used = min(cols, ((valid + CONV_K - 1) / CONV_K) * CONV_K + (cols - CONV_K * (int)blockDim.x));
     // each thread stages the D consecutive bins of a column (one or two cache
     // lines, read once), writing one element of every phase row
-    for (int col = tid; col < cols; col += blockDim.x) {
+    for (int col = tid; col < cols_used; col += blockDim.x) {
         const long long j0 = jbase + (long long)col * D;
         float2* dst = seg + (col & 3) * sub + (col >> 2);
         for (int ph = 0; ph < D; ph++) {
@@ -91,6 +96,7 @@ __global__ void __launch_bounds__(256)
         }
     }
     __syncthreads();
+    if (tid * CONV_K >= valid) return;   // no output of this thread (no barrier follows)
     float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
     for (int ph = 0; ph < D; ph++) {
         // element tid*4 + t + j of the phase row: sub-row j & 3, position tid + t/4 + j/4
@@ -145,20 +151,29 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
                                        int nd, const float2* demod, float2* out, cudaStream_t stream) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
     if (max_ph_taps % 4) return cudaErrorInvalidValue;
-    // smaller blocks for few lines, so that the grid still fills the GPU
-    int threads = 128;
-    while (threads > 32 && (int64_t)num_lines * ((nd + threads * CONV_K - 1) / (threads * CONV_K)) < 2 * 152) threads /= 2;
+    // a line's outputs split evenly over its blocks of at most 128 threads
+    // (4 outputs each; no block left nearly empty), and more blocks per line
+    // for few lines so that the grid still fills the GPU
+    auto threads_for = [&](int64_t blocks) {
+        const int64_t per = (nd + blocks - 1) / blocks;
+        return (int)std::max<int64_t>(32, ((per + CONV_K - 1) / CONV_K + 31) / 32 * 32);
+    };
+    int64_t nblk = (nd + 128 * CONV_K - 1) / (128 * CONV_K);
+    int threads = threads_for(nblk);
+    while (threads > 32 && (int64_t)num_lines * nblk < 2 * 152) threads = threads_for(++nblk);
+    nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
     auto smem_for = [&](int th, int taps_smem) {
         return ((size_t)4 * conv_sub(th, max_ph_taps) * decimation + (taps_smem ? (size_t)ntaps_pm : 0)) * sizeof(float2);
     };
     int taps_in_smem = 1;
     const size_t limit = 200 * 1024;
     if (smem_for(threads, 1) > limit) taps_in_smem = 0;   // very long windows: taps from global memory (broadcast loads)
-    while (smem_for(threads, taps_in_smem) > limit && threads > 32) threads /= 2;
+    while (smem_for(threads, taps_in_smem) > limit && threads > 32) threads -= 32;
     const size_t smem = smem_for(threads, taps_in_smem);
     if (smem > limit) return cudaErrorInvalidValue;
     const int sub = conv_sub(threads, max_ph_taps), cols = conv_cols(threads, max_ph_taps);
-    const dim3 grid((unsigned)((nd + threads * CONV_K - 1) / (threads * CONV_K)), (unsigned)num_lines);
+    nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
+    const dim3 grid((unsigned)nblk, (unsigned)num_lines);
     if (phase_delay) {
         auto k = convolve_demodulate_kernel<true>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
