@@ -512,23 +512,35 @@ def run_serve(args):
         s = gb.RfSimulator("gpu")
         gb.configure_job(s, j)
         sims.append(s)
-    server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4)
+    server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4, max_in_flight=args.max_in_flight)
     pids = [server.add_phantom(s) for s in sims]
     # warm-up: one request per phantom
     for k, s in enumerate(phantoms):
         sc = s.scan
         server.wait(server.submit(pids[k], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
                                   sc.timestamps, 8))
-    ids = []
+    # a client: this thread submits at the stream's arrival times, a second one
+    # collects the results in order as they complete
+    import queue
+
+    ids = queue.Queue()
+    lat = []
+
+    def collect():
+        for _ in range(len(reqs)):
+            lat.append(server.wait(ids.get())[1])
+
+    collector = threading.Thread(target=collect)
+    collector.start()
     t_start = time.perf_counter()
     for r in reqs:
         now = time.perf_counter() - t_start
         if r.arrival > now:
             time.sleep(r.arrival - now)
         sc = r.scan
-        ids.append(server.submit(pids[r.phantom], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
-                                 sc.timestamps, r.decimation))
-    lat = [server.wait(i)[1] for i in ids]
+        ids.put(server.submit(pids[r.phantom], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
+                              sc.timestamps, r.decimation))
+    collector.join()
     wall = time.perf_counter() - t_start
     st = server.stats()
     server.close()
@@ -553,16 +565,32 @@ def run_serve(args):
     def pct(v, q):
         return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
 
+    # where the tails come from: latency percentiles per phantom, and the slowest requests
+    per_phantom = {}
+    for k, ph in enumerate(phantoms):
+        idx = [i for i, r in enumerate(reqs) if r.phantom == k]
+        if not idx:
+            continue
+        a, b = sorted(lat[i] for i in idx), sorted(serial_lat[i] for i in idx)
+        per_phantom[ph.name] = {"requests": len(idx), "server_p50": pct(a, 0.5), "server_p99": pct(a, 0.99),
+                                "serial_p50": pct(b, 0.5), "serial_p99": pct(b, 0.99),
+                                "service_ms_mean": 1e3 * sum(service[i] for i in idx) / len(idx)}
+    slowest = sorted(range(len(reqs)), key=lambda i: -lat[i])[:8]
+    slow = [{"phantom": phantoms[reqs[i].phantom].name, "lines": reqs[i].scan.num_lines, "D": reqs[i].decimation,
+             "arrival_s": round(reqs[i].arrival, 4), "server_ms": lat[i], "serial_ms": serial_lat[i],
+             "service_ms": service[i] * 1e3} for i in slowest]
+
     return {"metric": METRIC + " (served stream)", "value": n_proj / wall, "unit": "projections/s",
             "n_gpus": 1, "steps": len(reqs), "warmup": len(phantoms), "ms_per_step": wall * 1e3 / max(1, len(reqs)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)",
             "data": "synthetic (seeded)",
             "config": {"workload": f"served_stream: {len(reqs)} requests, Poisson {args.rate}/s over "
-                                   f"{args.serve_seconds} s, 8 resident phantoms (scale {args.batch_scale})"},
+                                   f"{args.serve_seconds} s, 8 resident phantoms (scale {args.batch_scale})",
+                       "max_in_flight": args.max_in_flight},
             "latency_ms": {"p50": pct(lat_sorted, 0.5), "p99": pct(lat_sorted, 0.99), "max": lat_sorted[-1]},
             "serial_plain": {"latency_ms": {"p50": pct(ser_sorted, 0.5), "p99": pct(ser_sorted, 0.99)},
                              "busy_s": sum(service), "value": n_proj / sum(service)},
-            "server_stats": st}
+            "server_stats": st, "per_phantom": per_phantom, "slowest_requests": slow}
 
 
 def main():
@@ -584,6 +612,7 @@ def main():
     ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of N and L in batch/serve modes")
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--max-in-flight", type=int, default=3, help="serve mode: requests on the GPU at once")
     ap.add_argument("--simulate-only", action="store_true", help="only run warmup+steps simulations (profiling)")
     ap.add_argument("--traffic-bytes", type=float, default=None,
                     help="DRAM bytes per projection launch from an ncu capture (reported as roofline.traffic)")

@@ -166,17 +166,22 @@ int bcsim_batch_run_device(bcsim_batch* b, void* const* device_outs, const int64
  * simulate_lines at a time, e.g. src/qt5gui/MainWindow.cpp:656-735).
  * Phantoms -- configured handles: parameters, excitation, beam, scatterers --
  * are copied once and stay resident on the device.  Each request asks for
- * scan lines of one phantom.  A worker thread admits requests in arrival order
- * as simulator slots of their phantom free up, creating up to
- * max_slots_per_phantom slots while the device-memory budget allows, and runs
- * admitted requests concurrently on separate streams (continuous batching).
- * A request's IQ is identical to bcsim_simulate_lines of its phantom with its
- * lines, whatever else is in flight.
+ * scan lines of one phantom.  A worker thread admits requests strictly in
+ * arrival order while fewer than max_in_flight (default 3) are on the GPU and a
+ * simulator slot of their phantom is free -- up to max_slots_per_phantom slots
+ * while the device-memory budget allows, the first ones made and prepared when
+ * the phantom is added -- and runs admitted requests concurrently on separate
+ * streams (continuous batching: the host prepares the next request while the
+ * GPU runs the current ones).  A request's IQ is identical to
+ * bcsim_simulate_lines of its phantom with its lines, whatever else is in
+ * flight.
  * ------------------------------------------------------------------------- */
 typedef struct bcsim_server bcsim_server;
 int bcsim_server_create(int64_t hbm_budget_bytes, int max_slots_per_phantom, bcsim_server** out);
 int bcsim_server_destroy(bcsim_server* s);
 const char* bcsim_server_last_error(const bcsim_server* s);
+/* Requests on the GPU at once (>= 1; default 3). */
+int bcsim_server_set_max_in_flight(bcsim_server* s, int max_in_flight);
 /* Copies the configuration and scatterers of a configured handle; *phantom_id
  * identifies it in requests.  The handle stays the caller's. */
 int bcsim_server_add_phantom(bcsim_server* s, bcsim_handle* configured, int* phantom_id);

@@ -273,7 +273,7 @@ class Server:
     """Continuous-batching request server over resident phantoms
     (include/bcsim_gb300.h, bcsim_server_*)."""
 
-    def __init__(self, hbm_budget_bytes: int = 16 << 30, max_slots_per_phantom: int = 4):
+    def __init__(self, hbm_budget_bytes: int = 16 << 30, max_slots_per_phantom: int = 4, max_in_flight: int = 3):
         self._lib = _capi.load()
         s = C.c_void_p()
         rc = self._lib.bcsim_server_create(int(hbm_budget_bytes), int(max_slots_per_phantom), C.byref(s))
@@ -281,6 +281,7 @@ class Server:
             raise SimulatorError(rc, "bcsim_server_create failed")
         self._s = s
         self._shapes = {}
+        self._check(self._lib.bcsim_server_set_max_in_flight(self._s, int(max_in_flight)))
 
     def close(self):
         s = getattr(self, "_s", None)

@@ -50,6 +50,7 @@ SIGNATURES = [
     ("bcsim_server_create", C.c_int, [C.c_int64, C.c_int, C.POINTER(C.c_void_p)]),
     ("bcsim_server_destroy", C.c_int, [C.c_void_p]),
     ("bcsim_server_last_error", C.c_char_p, [C.c_void_p]),
+    ("bcsim_server_set_max_in_flight", C.c_int, [C.c_void_p, C.c_int]),
     ("bcsim_server_add_phantom", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     ("bcsim_server_submit", C.c_int, [C.c_void_p, C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float, C.c_int,
                                       _i64p]),

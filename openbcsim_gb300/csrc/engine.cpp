@@ -32,6 +32,7 @@ DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
         release();
         ptr_ = o.ptr_;
         bytes_ = o.bytes_;
+        stream_ = o.stream_;
         o.ptr_ = nullptr;
         o.bytes_ = 0;
     }
@@ -41,22 +42,30 @@ DeviceBuffer& DeviceBuffer::operator=(DeviceBuffer&& o) noexcept {
 DeviceBuffer::~DeviceBuffer() { release(); }
 
 void DeviceBuffer::release() {
-    if (ptr_) cudaFree(ptr_);
+    if (ptr_) {
+        if (stream_) cudaFreeAsync(ptr_, stream_);
+        else cudaFree(ptr_);
+    }
     ptr_ = nullptr;
     bytes_ = 0;
 }
 
-void DeviceBuffer::reserve(size_t bytes) {
+void DeviceBuffer::reserve(size_t bytes, cudaStream_t stream) {
     if (bytes <= bytes_ && ptr_) return;
+    // a buffer that has to grow grows by at least half, so that a sequence of
+    // slowly growing requests reallocates only a few times
+    if (ptr_) bytes = std::max(bytes, bytes_ + bytes_ / 2);
     release();
     if (bytes == 0) bytes = 16;
-    const cudaError_t e = cudaMalloc(&ptr_, bytes);
+    bytes = (bytes + 255) & ~(size_t)255;
+    const cudaError_t e = stream ? cudaMallocAsync(&ptr_, bytes, stream) : cudaMalloc(&ptr_, bytes);
     if (e != cudaSuccess) {
         ptr_ = nullptr;
         cudaGetLastError();
         throw SimError(BCSIM_E_MEMORY, std::string("device allocation of ") + std::to_string(bytes) +
                                            " bytes failed: " + cudaGetErrorString(e));
     }
+    stream_ = stream;
     bytes_ = bytes;
 }
 
@@ -79,9 +88,7 @@ static std::string fmt_double(double v) {
 
 Simulator::Simulator() = default;
 
-Simulator::~Simulator() {
-    if (stream_) cudaStreamDestroy(stream_);
-}
+Simulator::~Simulator() = default;   // buffers freed in stream order, then the stream (OwnedStream)
 
 void Simulator::log(int level, const std::string& msg) const {
     if (log_fn_) log_fn_(level, msg.c_str(), log_user_);
@@ -93,8 +100,24 @@ void Simulator::ensure_device() {
     BCSIM_CUDA(cudaGetDeviceCount(&count));
     if (device_ < 0 || device_ >= count) throw SimError(BCSIM_E_INVALID, "illegal CUDA device number");
     BCSIM_CUDA(cudaSetDevice(device_));
-    BCSIM_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&owned_stream_.s, cudaStreamNonBlocking));
+    stream_ = owned_stream_.s;
     device_ready_ = true;
+    {
+        // the device pool behind the stream-ordered buffers keeps freed memory
+        // for reuse instead of returning it at every synchronisation
+        static std::mutex pool_mu;
+        static bool pool_set[64] = {};
+        std::lock_guard<std::mutex> lock(pool_mu);
+        if (device_ < 64 && !pool_set[device_]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, device_) == cudaSuccess) {
+                uint64_t keep = UINT64_MAX;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            pool_set[device_] = true;
+        }
+    }
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, device_) == cudaSuccess) {
         std::ostringstream ss;
@@ -286,6 +309,21 @@ void Simulator::set_scan_sequence(const float* origins, const float* dirs, const
     cfg_version_++;
 }
 
+void Simulator::copy_scan_from(const Simulator& o) {
+    if (!o.scan_set_) return;
+    lines_ = o.lines_;
+    timestamps_ = o.timestamps_;
+    num_lines_ = o.num_lines_;
+    line_length_ = o.line_length_;
+    ns_ = num_rf_samples(sound_speed_, line_length_, fs_);
+    shared_origin_ = o.shared_origin_;
+    timestamps_equal_ = o.timestamps_equal_;
+    scan_set_ = true;
+    lines_valid_ = false;
+    tables_valid_ = false;
+    cfg_version_++;
+}
+
 void Simulator::set_analytical_profile(float sigma_lateral, float sigma_elevational) {
     cfg_version_++;
     log(1, "Setting analytical beam profile for GPU algorithm");
@@ -330,7 +368,7 @@ void Simulator::add_fixed_scatterers(const float* xyza, int64_t n) {
         const size_t need = (size_t)(fixed_n_ + n) * sizeof(float4);
         if (need > fixed_xyza_.bytes()) {
             DeviceBuffer grown;
-            grown.reserve(std::max(need, fixed_xyza_.bytes() * 3 / 2));
+            grown.reserve(std::max(need, fixed_xyza_.bytes() * 3 / 2), stream_);
             if (fixed_n_ > 0)
                 BCSIM_CUDA(cudaMemcpyAsync(grown.get(), fixed_xyza_.get(), (size_t)fixed_n_ * sizeof(float4),
                                            cudaMemcpyDeviceToDevice, stream_));
@@ -339,14 +377,15 @@ void Simulator::add_fixed_scatterers(const float* xyza, int64_t n) {
         }
         BCSIM_CUDA(cudaMemcpyAsync(fixed_xyza_.as<float4>() + fixed_n_, xyza, (size_t)n * sizeof(float4),
                                    cudaMemcpyHostToDevice, stream_));
+        // amplitude bound and finiteness on the device (the amplitude is the
+        // 4th float of every scatterer)
         double s = 0.0;
-        for (int64_t i = 0; i < n; i++) {
-            const float a = xyza[4 * i + 3];
-            if (!std::isfinite(a)) amplitude_nonfinite_ = true;
-            else s += std::fabs((double)a);
-        }
+        int bad = 0;
+        ingest_scratch_.reserve(abs_sum_scratch_bytes(), stream_);
+        BCSIM_CUDA(abs_sum(reinterpret_cast<const float*>(fixed_xyza_.as<float4>() + fixed_n_) + 3, 4, n,
+                           ingest_scratch_.get(), &s, &bad, stream_));
+        if (bad) amplitude_nonfinite_ = true;
         fixed_sum_abs_ += s;
-        BCSIM_CUDA(cudaStreamSynchronize(stream_));
     }
     fixed_n_ += n;
     num_fixed_sets_ += 1;
@@ -378,24 +417,23 @@ void Simulator::add_spline_scatterers(int degree, const float* knots, int num_kn
     ds.knots.assign(knots, knots + num_knots);
     ds.n = n;
     if (n > 0 && num_cs > 0) {
-        // [n][K][3] -> [K][n] float4
-        std::vector<float4> t((size_t)num_cs * n);
-        for (int64_t i = 0; i < n; i++)
-            for (int k = 0; k < num_cs; k++) {
-                const float* q = cps + (i * num_cs + k) * 3;
-                t[(size_t)k * n + i] = make_float4(q[0], q[1], q[2], 0.0f);
-            }
-        ds.cps.reserve(t.size() * sizeof(float4));
-        BCSIM_CUDA(cudaMemcpy(ds.cps.get(), t.data(), t.size() * sizeof(float4), cudaMemcpyHostToDevice));
+        // the caller's [n][K][3] as it is, laid out [K][n] float4 on the device
+        DeviceBuffer raw;
+        raw.reserve((size_t)n * num_cs * 3 * sizeof(float), stream_);
+        BCSIM_CUDA(cudaMemcpyAsync(raw.get(), cps, (size_t)n * num_cs * 3 * sizeof(float), cudaMemcpyHostToDevice,
+                                   stream_));
+        ds.cps.reserve((size_t)num_cs * n * sizeof(float4), stream_);
+        BCSIM_CUDA(launch_spline_transpose(raw.as<float>(), n, num_cs, ds.cps.as<float4>(), stream_));
     }
     if (n > 0) {
-        ds.amps.reserve((size_t)n * sizeof(float));
-        BCSIM_CUDA(cudaMemcpy(ds.amps.get(), amps, (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
-        for (int64_t i = 0; i < n; i++) {
-            if (!std::isfinite(amps[i])) amplitude_nonfinite_ = true;
-            else ds.sum_abs_amp += std::fabs((double)amps[i]);
-        }
+        ds.amps.reserve((size_t)n * sizeof(float), stream_);
+        BCSIM_CUDA(cudaMemcpyAsync(ds.amps.get(), amps, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, stream_));
+        int bad = 0;
+        ingest_scratch_.reserve(abs_sum_scratch_bytes(), stream_);
+        BCSIM_CUDA(abs_sum(ds.amps.as<float>(), 1, n, ingest_scratch_.get(), &ds.sum_abs_amp, &bad, stream_));
+        if (bad) amplitude_nonfinite_ = true;
     }
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));
     splines_.push_back(std::move(ds));
     cfg_version_++;
     data_version_++;
@@ -458,15 +496,15 @@ void Simulator::prepare_excitation_tables() {
                    std::to_string(M_));
     }
     const auto dm = demod_factors(fd_, fs_, decimation_, nd_, mode_ == MODE_REFERENCE);
-    demod_dev_.reserve(dm.size() * sizeof(float2));
+    demod_dev_.reserve(dm.size() * sizeof(float2), stream_);
     BCSIM_CUDA(cudaMemcpyAsync(demod_dev_.get(), dm.data(), dm.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     // the window's taps in the kernel's phase-major order for this decimation
     std::vector<float2> pm((size_t)tap_count_ + 4 * decimation_);
     std::vector<int> off((size_t)decimation_ + 1);
     ntaps_pm_ = make_phase_major_taps(fir_taps_host_.data(), (int)tap_count_, decimation_, pm.data(), off.data(),
                                       &max_ph_taps_);
-    taps_pm_dev_.reserve(std::max<size_t>(1, (size_t)ntaps_pm_) * sizeof(float2));
-    ph_off_dev_.reserve(off.size() * sizeof(int));
+    taps_pm_dev_.reserve(std::max<size_t>(1, (size_t)ntaps_pm_) * sizeof(float2), stream_);
+    ph_off_dev_.reserve(off.size() * sizeof(int), stream_);
     BCSIM_CUDA(cudaMemcpyAsync(taps_pm_dev_.get(), pm.data(), (size_t)ntaps_pm_ * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaMemcpyAsync(ph_off_dev_.get(), off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
@@ -591,7 +629,7 @@ static void order_lines(const std::vector<LineGeom>& lines, std::vector<int>& or
 
 void Simulator::prepare_lines() {
     if (lines_valid_) return;
-    lines_dev_.reserve(std::max<size_t>(1, lines_.size()) * sizeof(LineGeom));
+    lines_dev_.reserve(std::max<size_t>(1, lines_.size()) * sizeof(LineGeom), stream_);
     if (!lines_.empty())
         BCSIM_CUDA(cudaMemcpyAsync(lines_dev_.get(), lines_.data(), lines_.size() * sizeof(LineGeom),
                                    cudaMemcpyHostToDevice, stream_));
@@ -600,8 +638,8 @@ void Simulator::prepare_lines() {
     order_lines(lines_, order, cones);
     line_rank_.assign(order.size(), 0);
     for (size_t i = 0; i < order.size(); i++) line_rank_[order[i]] = (int)i;
-    line_order_dev_.reserve(std::max<size_t>(1, order.size()) * sizeof(int));
-    cones_dev_.reserve(std::max<size_t>(1, cones.size()) * sizeof(SlotCone));
+    line_order_dev_.reserve(std::max<size_t>(1, order.size()) * sizeof(int), stream_);
+    cones_dev_.reserve(std::max<size_t>(1, cones.size()) * sizeof(SlotCone), stream_);
     if (!order.empty()) {
         BCSIM_CUDA(cudaMemcpyAsync(line_order_dev_.get(), order.data(), order.size() * sizeof(int),
                                    cudaMemcpyHostToDevice, stream_));
@@ -704,7 +742,7 @@ void Simulator::prepare() {
     } else {
         if (!lut_uploaded_ || lut_packed_mode_ != mode_) {
             const auto packed = pack_lut(lut_, lut_nr_, lut_nl_, lut_ne_, mode_ == MODE_FP64);
-            lut4_.reserve(packed.size() * sizeof(float4));
+            lut4_.reserve(packed.size() * sizeof(float4), stream_);
             BCSIM_CUDA(cudaMemcpyAsync(lut4_.get(), packed.data(), packed.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
             BCSIM_CUDA(cudaStreamSynchronize(st));
             lut_uploaded_ = true;
@@ -801,6 +839,7 @@ void Simulator::prepare() {
                     lb.lo[j - lo] = mode_ == MODE_FP64 ? (float)(v - (double)hi) : 0.0f;
                 }
             }
+            lb.mu = mu;
             mus[d][i] = mu;
             bases[d][i] = lb;
         }
@@ -819,8 +858,10 @@ void Simulator::prepare() {
         }
     }
 
-    // lines of a per-pair tile: same knot interval (splines), nearby directions
-    auto make_tiles = [&](const std::vector<int>* mu, std::vector<int>& ids, std::vector<LineTile>& tiles) {
+    // lines of a per-pair tile: sorted by knot interval (splines), then by
+    // direction; a tile of splines spans at most 64 control points (so that the
+    // kernel stages at least 32 scatterers per chunk)
+    auto make_tiles = [&](const std::vector<int>* mu, int degree, std::vector<int>& ids, std::vector<LineTile>& tiles) {
         ids.resize(L);
         std::iota(ids.begin(), ids.end(), 0);
         std::sort(ids.begin(), ids.end(), [&](int a, int c) {
@@ -834,10 +875,10 @@ void Simulator::prepare() {
             LineTile t;
             t.first = i;
             t.mu = mu ? (*mu)[ids[i]] : 0;
-            t.pad = 0;
             int j = i;
-            while (j < L && j - i < per && (!mu || (*mu)[ids[j]] == t.mu)) j++;
+            while (j < L && j - i < per && (!mu || (*mu)[ids[j]] - t.mu + degree + 1 <= 64)) j++;
             t.count = j - i;
+            t.span = mu ? (*mu)[ids[j - 1]] - t.mu + degree + 1 : 1;
             tiles.push_back(t);
             i = j;
         }
@@ -848,7 +889,7 @@ void Simulator::prepare() {
     auto add_gen = [&](int kind, int d) {
         std::vector<int> ids;
         std::vector<LineTile> tiles;
-        make_tiles(kind == 1 ? &mus[d] : nullptr, ids, tiles);
+        make_tiles(kind == 1 ? &mus[d] : nullptr, kind == 1 ? splines_[d].degree : 0, ids, tiles);
         GenLaunch g;
         g.kind = kind;
         g.d = d;
@@ -865,9 +906,9 @@ void Simulator::prepare() {
     if (fixed_n_ > 0) add_gen(0, -1);
     for (size_t d = 0; d < splines_.size(); d++)
         if (splines_[d].n > 0) add_gen(1, (int)d);
-    gen_tiles_.reserve(std::max<size_t>(1, all_tiles.size()) * sizeof(LineTile));
-    gen_line_ids_.reserve(std::max<size_t>(1, all_ids.size()) * sizeof(int));
-    gen_basis_.reserve(std::max<size_t>(1, all_basis.size()) * sizeof(LineBasis));
+    gen_tiles_.reserve(std::max<size_t>(1, all_tiles.size()) * sizeof(LineTile), stream_);
+    gen_line_ids_.reserve(std::max<size_t>(1, all_ids.size()) * sizeof(int), stream_);
+    gen_basis_.reserve(std::max<size_t>(1, all_basis.size()) * sizeof(LineBasis), stream_);
     if (!all_tiles.empty())
         BCSIM_CUDA(cudaMemcpyAsync(gen_tiles_.get(), all_tiles.data(), all_tiles.size() * sizeof(LineTile), cudaMemcpyHostToDevice, st));
     if (!all_ids.empty())
@@ -878,20 +919,20 @@ void Simulator::prepare() {
     // device buffers
     const int stride = phase_delay_ ? 2 : 1;
     P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
-    bins_.reserve(P.bins_bytes);
-    counts_.reserve(4 * sizeof(int));
-    pair_counts_.reserve(3 * sizeof(unsigned long long));
-    out_.reserve((size_t)L * nd_ * sizeof(float2));
+    bins_.reserve(P.bins_bytes, stream_);
+    counts_.reserve(4 * sizeof(int), stream_);
+    pair_counts_.reserve(3 * sizeof(unsigned long long), stream_);
+    out_.reserve((size_t)L * nd_ * sizeof(float2), stream_);
     P.spline_off.assign(splines_.size(), -1);
     if (P.n_shared > 0) {
         const int64_t N = P.n_shared;
-        keys_in_.reserve(N * sizeof(uint32_t));
-        vals_in_.reserve(N * sizeof(uint32_t));
-        keys_out_.reserve(N * sizeof(uint32_t));
-        vals_out_.reserve(N * sizeof(uint32_t));
-        recA_.reserve(N * sizeof(float4));
-        recB_.reserve(N * sizeof(float4));
-        records_.reserve((size_t)N * 2 * sizeof(float4));
+        keys_in_.reserve(N * sizeof(uint32_t), stream_);
+        vals_in_.reserve(N * sizeof(uint32_t), stream_);
+        keys_out_.reserve(N * sizeof(uint32_t), stream_);
+        vals_out_.reserve(N * sizeof(uint32_t), stream_);
+        recA_.reserve(N * sizeof(float4), stream_);
+        recB_.reserve(N * sizeof(float4), stream_);
+        records_.reserve((size_t)N * 2 * sizeof(float4), stream_);
         int64_t off = fixed_n_;
         std::vector<double> bd(64 * std::max<size_t>(1, splines_.size()), 0.0);
         std::vector<float> bf(64 * std::max<size_t>(1, splines_.size()), 0.0f);
@@ -909,8 +950,8 @@ void Simulator::prepare() {
             P.spline_first_cs[d] = lo;
             off += ds.n;
         }
-        spl_basis_d_.reserve(bd.size() * sizeof(double));
-        spl_basis_f_.reserve(bf.size() * sizeof(float));
+        spl_basis_d_.reserve(bd.size() * sizeof(double), stream_);
+        spl_basis_f_.reserve(bf.size() * sizeof(float), stream_);
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_d_.get(), bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_f_.get(), bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
         int end_bit = 1;
@@ -919,7 +960,7 @@ void Simulator::prepare() {
         size_t tmp_bytes = 0;
         BCSIM_CUDA(radix_sort_pairs(nullptr, &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
                                     vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
-        sort_tmp_.reserve(tmp_bytes);
+        sort_tmp_.reserve(tmp_bytes, stream_);
         P.sort_tmp_bytes = tmp_bytes;
         // records per CTA (a multiple of 128 so that results do not depend on it):
         // enough CTAs to fill the GPU several times over
@@ -1111,7 +1152,7 @@ void Simulator::autotune() {
     std::vector<int> chunks = {P.chunk};
     if (P.n_shared > 0) chunks = {128, 256, 512, 1024};
     const cudaStream_t st = stream_;
-    out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2));
+    out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2), stream_);
     cudaEvent_t e0, e1;
     BCSIM_CUDA(cudaEventCreate(&e0));
     BCSIM_CUDA(cudaEventCreate(&e1));
@@ -1149,7 +1190,7 @@ void Simulator::simulate_host(float* host_out, int64_t cap_complex, int64_t* lin
     if (!host_out || cap_complex < L * nd)
         throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
     ensure_device();
-    out_.reserve((size_t)L * nd * sizeof(float2));
+    out_.reserve((size_t)L * nd * sizeof(float2), stream_);
     simulate(out_.as<float2>(), host_out);
 }
 
@@ -1199,8 +1240,9 @@ void Simulator::clone_from(Simulator& o) {
     fixed_sum_abs_ = o.fixed_sum_abs_;
     amplitude_nonfinite_ = o.amplitude_nonfinite_;
     if (fixed_n_ > 0) {
-        fixed_xyza_.reserve((size_t)fixed_n_ * sizeof(float4));
-        BCSIM_CUDA(cudaMemcpy(fixed_xyza_.get(), o.fixed_xyza_.get(), (size_t)fixed_n_ * sizeof(float4), cudaMemcpyDeviceToDevice));
+        fixed_xyza_.reserve((size_t)fixed_n_ * sizeof(float4), stream_);
+        BCSIM_CUDA(cudaMemcpyAsync(fixed_xyza_.get(), o.fixed_xyza_.get(), (size_t)fixed_n_ * sizeof(float4),
+                                   cudaMemcpyDeviceToDevice, stream_));
     }
     splines_.clear();
     for (const SplineDataset& src : o.splines_) {
@@ -1211,15 +1253,18 @@ void Simulator::clone_from(Simulator& o) {
         ds.n = src.n;
         ds.sum_abs_amp = src.sum_abs_amp;
         if (src.n > 0 && src.num_cs > 0) {
-            ds.cps.reserve((size_t)src.num_cs * src.n * sizeof(float4));
-            BCSIM_CUDA(cudaMemcpy(ds.cps.get(), src.cps.get(), (size_t)src.num_cs * src.n * sizeof(float4), cudaMemcpyDeviceToDevice));
+            ds.cps.reserve((size_t)src.num_cs * src.n * sizeof(float4), stream_);
+            BCSIM_CUDA(cudaMemcpyAsync(ds.cps.get(), src.cps.get(), (size_t)src.num_cs * src.n * sizeof(float4),
+                                       cudaMemcpyDeviceToDevice, stream_));
         }
         if (src.n > 0) {
-            ds.amps.reserve((size_t)src.n * sizeof(float));
-            BCSIM_CUDA(cudaMemcpy(ds.amps.get(), src.amps.get(), (size_t)src.n * sizeof(float), cudaMemcpyDeviceToDevice));
+            ds.amps.reserve((size_t)src.n * sizeof(float), stream_);
+            BCSIM_CUDA(cudaMemcpyAsync(ds.amps.get(), src.amps.get(), (size_t)src.n * sizeof(float),
+                                       cudaMemcpyDeviceToDevice, stream_));
         }
         splines_.push_back(std::move(ds));
     }
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));
     scan_set_ = false;
     tables_valid_ = false;
     lines_valid_ = false;

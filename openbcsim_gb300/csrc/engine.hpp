@@ -27,16 +27,22 @@ struct SimError : public std::runtime_error {
     SimError(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
 };
 
-// Owning device allocation that only grows.
+// Owning device allocation that only grows.  With a stream it is allocated and
+// freed in that stream's order from the device's memory pool (no device-wide
+// synchronisation, as cudaFree would cause: a simulator that serves requests
+// of changing size never stalls the other streams); growth is geometric.
 class DeviceBuffer {
 public:
     DeviceBuffer() = default;
     DeviceBuffer(const DeviceBuffer&) = delete;
     DeviceBuffer& operator=(const DeviceBuffer&) = delete;
-    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_) { o.ptr_ = nullptr; o.bytes_ = 0; }
+    DeviceBuffer(DeviceBuffer&& o) noexcept : ptr_(o.ptr_), bytes_(o.bytes_), stream_(o.stream_) {
+        o.ptr_ = nullptr;
+        o.bytes_ = 0;
+    }
     DeviceBuffer& operator=(DeviceBuffer&& o) noexcept;
     ~DeviceBuffer();
-    void reserve(size_t bytes);   // grow (contents not kept)
+    void reserve(size_t bytes, cudaStream_t stream = nullptr);   // grow (contents not kept)
     void release();
     void* get() const { return ptr_; }
     template <typename T> T* as() const { return static_cast<T*>(ptr_); }
@@ -45,6 +51,23 @@ public:
 private:
     void* ptr_ = nullptr;
     size_t bytes_ = 0;
+    cudaStream_t stream_ = nullptr;   // stream-ordered allocation on this stream (null: cudaMalloc)
+};
+
+// A simulator's stream, destroyed (after its work) when the simulator goes --
+// declared before the simulator's buffers, so that those are freed first, in
+// its order.
+struct OwnedStream {
+    cudaStream_t s = nullptr;
+    OwnedStream() = default;
+    OwnedStream(const OwnedStream&) = delete;
+    OwnedStream& operator=(const OwnedStream&) = delete;
+    ~OwnedStream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
 };
 
 struct SplineDataset {
@@ -119,6 +142,8 @@ public:
     // Copy the whole configuration of o (parameters, excitation, beam, scatterer
     // datasets -- device copies; not the scan sequence) into this simulator.
     void clone_from(Simulator& o);
+    // Take o's scan sequence (after clone_from, whose configuration it needs).
+    void copy_scan_from(const Simulator& o);
     // Device bytes this simulator holds or will hold for num_lines lines of ns samples.
     size_t footprint_bytes(int num_lines, int64_t ns) const;
     // Samples per line this configuration gives for a line length.
@@ -147,7 +172,8 @@ private:
     // configuration
     int device_ = 0;
     bool device_ready_ = false;
-    cudaStream_t stream_ = nullptr;
+    OwnedStream owned_stream_;
+    cudaStream_t stream_ = nullptr;   // owned_stream_.s
     int verbose_ = 0;
     float sound_speed_ = 1540.0f;
     float noise_amplitude_ = 0.0f;
@@ -168,6 +194,7 @@ private:
     bool count_pairs_ = false;   // instrumented shared-origin kernel: visited / non-zero (record, line) pairs
     int last_launches_ = 0;      // kernels of this library launched by the last enqueue
     DeviceBuffer pair_counts_;
+    DeviceBuffer ingest_scratch_;   // amplitude reductions of add_*_scatterers
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
     uint64_t data_version_ = 1;  // bumped by every scatterer change
     uint64_t records_key_ = 0;

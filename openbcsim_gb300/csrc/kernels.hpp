@@ -71,12 +71,14 @@ struct SlotCone {
 };
 
 // A tile of lines for the per-pair projection kernel: `count` lines taken from
-// line_ids[first ...], all sharing the spline knot interval `mu`.
+// line_ids[first ...].  For splines the tile's lines need control points
+// mu - degree .. mu - degree + span - 1 (the union of their windows; lines are
+// sorted by knot interval, so a tile spans few intervals).
 struct LineTile {
     int first;
     int count;
-    int mu;
-    int pad;
+    int mu;     // smallest knot interval of the tile's lines
+    int span;   // control points staged per scatterer
 };
 
 // Lines per CTA of the per-pair kernel (the largest line tile).
@@ -88,6 +90,7 @@ constexpr int MAX_SPLINE_DEGREE = 7;
 struct LineBasis {
     float hi[MAX_SPLINE_DEGREE + 1];
     float lo[MAX_SPLINE_DEGREE + 1];
+    int mu;   // knot interval
 };
 
 // Shared-origin records, in bin order, as two planes of float4:
@@ -171,5 +174,15 @@ cudaError_t radix_sort_pairs(void* temp, size_t* temp_bytes, const uint32_t* key
 
 namespace bcsim_gb300 {
 // Reads and clears the device flag that a bounded wait sets when it gives up.
+// Scatterer ingestion (ingest.cu).  Spline control points [n][num_cs][3] ->
+// [num_cs][n] float4 (x, y, z, 0).
+cudaError_t launch_spline_transpose(const float* raw, int64_t n, int num_cs, float4* out, cudaStream_t stream);
+// Sum of |vals[i * stride]| over i < n (double, fixed reduction order) and
+// whether any value is not finite, into *sum / *nonfinite; synchronises the
+// stream.  scratch: abs_sum_scratch_bytes() of device memory.
+size_t abs_sum_scratch_bytes();
+cudaError_t abs_sum(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
+                    cudaStream_t stream);
+
 cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream);
 }

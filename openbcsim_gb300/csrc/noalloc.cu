@@ -171,7 +171,7 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
         t.first = i;
         t.count = num_lines - i < PAIR_THREADS ? num_lines - i : PAIR_THREADS;
         t.mu = 0;
-        t.pad = 0;
+        t.span = 1;
         g_tiles[num_tiles++] = t;
     }
 

@@ -732,9 +732,10 @@ __device__ __forceinline__ bool pair_bin(df dx, df dy, df dz, float dot, const S
 }
 
 // Per (scatterer, line) pair projection for any line geometry and for splines.
-// CTA = a tile of up to PAIR_THREADS lines (one per thread; for splines all with
-// the same knot interval mu) x a chunk of PAIR_CHUNK scatterers staged in shared
-// memory and broadcast to the threads.  Each pair first gets an FP32 position
+// CTA = a tile of up to PAIR_THREADS lines (one per thread; for splines sorted
+// by knot interval) x a chunk of scatterers staged in shared memory and
+// broadcast to the threads (for splines the tile's window of control points per
+// scatterer, each line reading its own p+1 of them).  Each pair first gets an FP32 position
 // and weight; a pair whose contribution rounds to zero in the fixed-point bins
 // (or lies outside the lookup table by a margin) is skipped -- exactly, since it
 // would add 0 -- and only the remaining pairs compute the float-pair time of
@@ -757,6 +758,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     }
     const int tid = threadIdx.x;
     const int np = degree + 1;
+    // control points staged per scatterer, and scatterers per chunk so that
+    // they fit the shared array
+    const int span = SPLINE ? tile.span : 1;
+    const int chunk = SPLINE ? min(PAIR_CHUNK, PAIR_CHUNK * (MAX_SPLINE_DEGREE + 1) / span) : PAIR_CHUNK;
     const bool active = tid < tile.count;
     const int line = __ldg(line_ids + tile.first + (active ? tid : 0));
     const LineGeom* g = lines + line;
@@ -765,8 +770,10 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
     const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
     float bh[MAX_SPLINE_DEGREE + 1], bl[MAX_SPLINE_DEGREE + 1];
+    int win = 0;   // this line's first control point within the staged window
     if (SPLINE) {
         const LineBasis* lb = basis + line;
+        win = __ldg(&lb->mu) - tile.mu;
 #pragma unroll
         for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
             bh[k] = k < np ? __ldg(&lb->hi[k]) : 0.0f;
@@ -779,8 +786,8 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const float skip_below = 0.499f / p.scale;
     const float gl = b.gl, ge = b.ge;
 
-    for (int64_t c0 = (int64_t)blockIdx.x * PAIR_CHUNK; c0 < count; c0 += (int64_t)gridDim.x * PAIR_CHUNK) {
-    const int cnt = (int)min((int64_t)PAIR_CHUNK, count - c0);
+    for (int64_t c0 = (int64_t)blockIdx.x * chunk; c0 < count; c0 += (int64_t)gridDim.x * chunk) {
+    const int cnt = (int)min((int64_t)chunk, count - c0);
     __syncthreads();   // the previous chunk is consumed
     // stage the chunk (gathering through the index list for the near-origin residue)
     for (int i = tid; i < cnt; i += blockDim.x) {
@@ -791,8 +798,8 @@ __global__ void __launch_bounds__(PAIR_THREADS)
             ok = s >= 0 && s < n;
         }
         if (SPLINE) {
-            for (int k = 0; k < np; k++)
-                sp[i * np + k] = ok ? __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s) : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int k = 0; k < span; k++)
+                sp[i * span + k] = ok ? __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s) : make_float4(0.f, 0.f, 0.f, 0.f);
             sa[i] = ok ? __ldg(amps + s) : 0.0f;
         } else {
             const float4 q = ok ? __ldg(xyza + s) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -815,7 +822,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 #pragma unroll
                 for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
                     if (k < np) {
-                        const float4 c = sp[i * np + k];
+                        const float4 c = sp[i * span + win + k];
                         fx = fmaf(bh[k], c.x, fx); fy = fmaf(bh[k], c.y, fy); fz = fmaf(bh[k], c.z, fz);
                     }
                 }
@@ -845,7 +852,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 #pragma unroll
                 for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
                     if (k < np) {
-                        const float4 c = sp[i * np + k];
+                        const float4 c = sp[i * span + win + k];
                         const df px = two_prod(bh[k], c.x), py = two_prod(bh[k], c.y), pz = two_prod(bh[k], c.z);
                         const df tx = two_sum(sx.hi, px.hi), ty = two_sum(sy.hi, py.hi), tz = two_sum(sz.hi, pz.hi);
                         sx.hi = tx.hi; sy.hi = ty.hi; sz.hi = tz.hi;
@@ -903,7 +910,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
 #pragma unroll
                 for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
                     if (k < np) {
-                        const float4 c = sp[i * np + k];
+                        const float4 c = sp[i * span + win + k];
                         sx = __fadd_rn(sx, __fmul_rn(c.x, bh[k]));
                         sy = __fadd_rn(sy, __fmul_rn(c.y, bh[k]));
                         sz = __fadd_rn(sz, __fmul_rn(c.z, bh[k]));

@@ -7,9 +7,12 @@
 // their phantom is free -- creating slots while the device-memory budget allows
 // -- prepares them on the host and enqueues their device work on the slot's own
 // stream, so requests that arrive while others are on the GPU overlap with them.
-// The same thread polls completion events, copies results out and records the
-// submit-to-result latency.  A request's result depends only on its phantom and
-// its own lines, never on what else is in flight.
+// The same thread polls completion events, hands each result (the pinned buffer
+// the device copied it to) to its request and records the submit-to-result
+// latency; the waiter copies it out.  Device buffers grow in stream order and
+// pinned buffers are recycled, so the steady state allocates nothing.  A
+// request's result depends only on its phantom and its own lines, never on what
+// else is in flight.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,11 +49,13 @@ struct Request {
     float line_length;
     int decimation;
     Clock::time_point submitted;
-    // result
+    // result: the pinned staging buffer the device copied it to, handed over
+    // by the slot (returned to the server's free list by the waiter)
     bool done = false;
     int status = BCSIM_OK;
     std::string error;
-    std::vector<float2> iq;
+    float2* iq = nullptr;
+    size_t iq_bytes = 0;
     int64_t nd = 0;
     double latency_ms = 0.0;
     int64_t projections = 0;
@@ -77,6 +82,7 @@ struct bcsim_server {
     int device = 0;
     int64_t budget = 0;
     int max_slots = 4;
+    std::atomic<int> max_in_flight{3};
     std::atomic<int64_t> in_use{0};
     // phantoms: fixed capacity so that the worker can read entries while
     // add_phantom appends (entries never move)
@@ -91,6 +97,7 @@ struct bcsim_server {
     int64_t next_id = 1;
     int64_t completed = 0, failed = 0, projections = 0;
     std::vector<double> latencies;
+    std::vector<std::pair<float2*, size_t>> free_pinned;   // result buffers returned by waiters
     bool stop = false;
     std::thread worker;
     std::string last_error;
@@ -98,7 +105,33 @@ struct bcsim_server {
     void run();
     bool dispatch(const std::shared_ptr<Request>& r);
     void poll();
+    int busy_slots();
 };
+
+namespace {
+// A slot: a simulator holding a copy of the phantom, its result staging and its
+// completion event.
+std::unique_ptr<Slot> make_slot(Simulator& base, size_t bytes) {
+    auto s = std::make_unique<Slot>();
+    s->sim = std::make_unique<Simulator>();
+    s->sim->clone_from(base);
+    s->bytes = bytes;
+    if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess)
+        throw SimError(BCSIM_E_CUDA, "cudaEventCreate failed");
+    const size_t pinned = (size_t)8 << 20;
+    if (cudaMallocHost(&s->host, pinned) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
+    s->host_bytes = pinned;
+    return s;
+}
+}  // namespace
+
+int bcsim_server::busy_slots() {
+    int n = 0;
+    const int np = num_phantoms.load();
+    for (int pi = 0; pi < np; pi++)
+        for (auto& s : phantoms[pi]->slots) n += s->busy ? 1 : 0;
+    return n;
+}
 
 bool bcsim_server::dispatch(const std::shared_ptr<Request>& r) {
     Phantom& ph = *phantoms[r->phantom];
@@ -109,14 +142,8 @@ bool bcsim_server::dispatch(const std::shared_ptr<Request>& r) {
     if (!slot) {
         const size_t need = ph.base->footprint_bytes(r->num_lines, ns);
         if ((int)ph.slots.size() >= max_slots || (!ph.slots.empty() && in_use + (int64_t)need > budget)) return false;
-        auto s = std::make_unique<Slot>();
-        s->sim = std::make_unique<Simulator>();
-        s->sim->clone_from(*ph.base);
-        s->bytes = need;
+        ph.slots.push_back(make_slot(*ph.base, need));
         in_use += (int64_t)need;
-        if (cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming) != cudaSuccess)
-            throw SimError(BCSIM_E_CUDA, "cudaEventCreate failed");
-        ph.slots.push_back(std::move(s));
         slot = ph.slots.back().get();
     }
     slot->busy = true;
@@ -129,10 +156,14 @@ bool bcsim_server::dispatch(const std::shared_ptr<Request>& r) {
         sim.prepare();
         const size_t bytes = (size_t)sim.num_lines() * sim.num_out_samples() * sizeof(float2);
         if (bytes > slot->host_bytes) {
+            // pinned staging grows rarely (at least 8 MiB, then doubling): freeing
+            // pinned memory can wait for the device
+            const size_t grow = std::max({bytes, slot->host_bytes * 2, (size_t)8 << 20});
             if (slot->host) cudaFreeHost(slot->host);
             slot->host = nullptr;
-            if (cudaMallocHost(&slot->host, bytes) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
-            slot->host_bytes = bytes;
+            slot->host_bytes = 0;
+            if (cudaMallocHost(&slot->host, grow) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
+            slot->host_bytes = grow;
         }
         cudaStream_t st = sim.stream();
         sim.enqueue(st, sim.internal_output(), false);
@@ -162,11 +193,19 @@ void bcsim_server::poll() {
             const cudaError_t q = cudaEventQuery(s->done);
             if (q == cudaErrorNotReady) continue;
             std::shared_ptr<Request> r = s->req;
-            const size_t n = (size_t)r->num_lines * r->nd;
-            std::vector<float2> iq(s->host, s->host + n);
             std::lock_guard<std::mutex> lock(mu);
             if (q == cudaSuccess) {
-                r->iq.swap(iq);
+                // hand the staging buffer to the request; the slot takes a
+                // returned one (or allocates at its next dispatch)
+                r->iq = s->host;
+                r->iq_bytes = s->host_bytes;
+                s->host = nullptr;
+                s->host_bytes = 0;
+                if (!free_pinned.empty()) {
+                    s->host = free_pinned.back().first;
+                    s->host_bytes = free_pinned.back().second;
+                    free_pinned.pop_back();
+                }
                 r->latency_ms = std::chrono::duration<double, std::milli>(Clock::now() - r->submitted).count();
                 latencies.push_back(r->latency_ms);
                 completed++;
@@ -198,9 +237,14 @@ void bcsim_server::run() {
             if (stop && pending.empty() && !any_busy) return;
             todo.assign(pending.begin(), pending.end());
         }
-        // admit in arrival order; a request whose phantom has no free slot waits
+        // admit strictly in arrival order while fewer than max_in_flight
+        // requests are on the GPU: the GPU works on the oldest requests (their
+        // kernels overlap, and the host prepares the next request meanwhile)
+        // instead of sharing itself among every queued one
         std::vector<int64_t> admitted;
+        int in_flight = busy_slots();
         for (auto& r : todo) {
+            if (in_flight >= max_in_flight.load()) break;
             bool ok = false;
             try {
                 ok = dispatch(r);
@@ -213,7 +257,9 @@ void bcsim_server::run() {
                 ok = true;
                 done_cv.notify_all();
             }
-            if (ok) admitted.push_back(r->id);
+            if (!ok) break;   // its phantom has no free slot: later requests wait too
+            admitted.push_back(r->id);
+            in_flight++;
         }
         if (!admitted.empty()) {
             std::lock_guard<std::mutex> lock(mu);
@@ -224,7 +270,7 @@ void bcsim_server::run() {
                           pending.end());
         }
         poll();
-        if (admitted.empty()) std::this_thread::sleep_for(std::chrono::microseconds(50));
+        if (admitted.empty()) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -276,18 +322,44 @@ int bcsim_server_destroy(bcsim_server* s) {
             if (sl->host) cudaFreeHost(sl->host);
             if (sl->done) cudaEventDestroy(sl->done);
         }
+    for (auto& b : s->free_pinned) cudaFreeHost(b.first);
+    for (auto& kv : s->requests)   // results never collected
+        if (kv.second->iq) cudaFreeHost(kv.second->iq);
     delete s;
     return BCSIM_OK;
 }
 
 const char* bcsim_server_last_error(const bcsim_server* s) { return s ? s->last_error.c_str() : "null server"; }
 
+int bcsim_server_set_max_in_flight(bcsim_server* s, int max_in_flight) {
+    if (!s || max_in_flight <= 0) return BCSIM_E_INVALID;
+    s->max_in_flight.store(max_in_flight);
+    return BCSIM_OK;
+}
+
 int bcsim_server_add_phantom(bcsim_server* s, bcsim_handle* configured, int* phantom_id) {
     return guarded(s, [&] {
         if (!configured || !phantom_id) throw SimError(BCSIM_E_INVALID, "null argument");
         auto ph = std::make_unique<Phantom>();
+        Simulator& src = bcsim_gb300::simulator_of(configured);
         ph->base = std::make_unique<Simulator>();
-        ph->base->clone_from(bcsim_gb300::simulator_of(configured));
+        ph->base->clone_from(src);
+        // slots made now, and prepared once with the handle's scan (when it has
+        // one): device buffers, tables and staging exist before the first request
+        const int warm = std::min(s->max_slots, 3);
+        for (int k = 0; k < warm; k++) {
+            const size_t need = ph->base->footprint_bytes(1, 1);
+            if (k > 0 && s->in_use + (int64_t)need > s->budget) break;
+            ph->slots.push_back(make_slot(*ph->base, need));
+            s->in_use += (int64_t)need;
+            Simulator& sim = *ph->slots.back()->sim;
+            sim.copy_scan_from(src);
+            try {
+                sim.prepare();
+            } catch (const SimError&) {
+                // a scan that does not suit (e.g. none): the first request prepares
+            }
+        }
         std::lock_guard<std::mutex> lock(s->mu);
         const int id = s->num_phantoms.load();
         if (id >= bcsim_server::kMaxPhantoms) throw SimError(BCSIM_E_CAPACITY, "too many phantoms (256)");
@@ -350,11 +422,17 @@ int bcsim_server_wait(bcsim_server* s, int64_t request_id, float* out, int64_t c
     if (num_samples) *num_samples = r->nd;
     if (latency_ms) *latency_ms = r->latency_ms;
     const int64_t n = (int64_t)r->num_lines * r->nd;
+    int rc = BCSIM_OK;
     if (out) {
-        if (cap_complex < n) return BCSIM_E_CAPACITY;
-        std::memcpy(out, r->iq.data(), (size_t)n * sizeof(float2));
+        if (cap_complex < n) rc = BCSIM_E_CAPACITY;
+        else std::memcpy(out, r->iq, (size_t)n * sizeof(float2));
     }
-    return BCSIM_OK;
+    if (r->iq) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->free_pinned.emplace_back(r->iq, r->iq_bytes);
+        r->iq = nullptr;
+    }
+    return rc;
 }
 
 int bcsim_server_stats(bcsim_server* s, int64_t* completed, int64_t* failed, double* p50_ms, double* p99_ms,
