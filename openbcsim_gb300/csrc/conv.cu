@@ -35,34 +35,39 @@ namespace bcsim_gb300 {
 
 constexpr int CONV_K = 4;   // outputs per thread
 
-__device__ __forceinline__ void cmac(float2& y, float2 v, float2 h) {
-    y.x = fmaf(v.x, h.x, fmaf(-v.y, h.y, y.x));
-    y.y = fmaf(v.x, h.y, fmaf(v.y, h.x, y.y));
+// Complex multiply-accumulate y += v h with paired FP32 FMAs (two per
+// instruction): the tap is held as (h.re, h.im, -h.im, h.re), so that
+//     y += (v.im, v.im) * (-h.im, h.re),   y += (v.re, v.re) * (h.re, h.im)
+// are two FFMA2 -- per component the same two fused operations, in the same
+// order, as fma(v.re, h.re, fma(-v.im, h.im, y.re)) and its imaginary twin.
+__device__ __forceinline__ void cmac(float2& y, float2 v, float4 h) {
+    y = __ffma2_rn(make_float2(v.y, v.y), make_float2(h.z, h.w), y);
+    y = __ffma2_rn(make_float2(v.x, v.x), make_float2(h.x, h.y), y);
 }
-__device__ __forceinline__ void rmac(float2& y, float2 v, float2 h) {
-    y.x = fmaf(v.x, h.x, y.x);
-    y.y = fmaf(v.x, h.y, y.y);
+// real bins (no phase delay): y += v.re h
+__device__ __forceinline__ void rmac(float2& y, float2 v, float4 h) {
+    y = __ffma2_rn(make_float2(v.x, v.x), make_float2(h.x, h.y), y);
 }
+__device__ __forceinline__ float4 tap4(float2 h) { return make_float4(h.x, h.y, -h.y, h.x); }
 
-template <bool PD>
-__global__ void __launch_bounds__(256)
+template <bool PD, bool TAPS_SMEM>
+__global__ void __launch_bounds__(128)
     convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
                                const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
                                int tap_start, int64_t M, int center, int D, int nd, int sub, int cols,
-                               int taps_in_smem, const float2* __restrict__ demod, float2* __restrict__ out) {
-    extern __shared__ float2 smem[];
-    float2* seg = smem;                               // [D][4][sub]
+                               const float2* __restrict__ demod, float2* __restrict__ out) {
+    extern __shared__ float4 smem4[];
+    float2* seg = reinterpret_cast<float2*>(smem4);   // [D][4][sub]
     const int row = 4 * sub;
-    const float2* tp = taps_pm;                       // phase-major taps (shared memory when they fit)
+    // phase-major taps as (h.re, h.im, -h.im, h.re), in shared memory when they fit
+    float4* tp4 = reinterpret_cast<float4*>(seg + (size_t)D * row);
     const int line = blockIdx.y;
     const int per_cta = blockDim.x * CONV_K;
     const int m0 = blockIdx.x * per_cta;
     const int tid = threadIdx.x;
-    if (taps_in_smem) {
-        float2* t = smem + (size_t)D * row;
+    if (TAPS_SMEM) {
         const int ntaps_pm = __ldg(ph_off + D);
-        for (int i = tid; i < ntaps_pm; i += blockDim.x) t[i] = __ldg(taps_pm + i);
-        tp = t;
+        for (int i = tid; i < ntaps_pm; i += blockDim.x) tp4[i] = tap4(__ldg(taps_pm + i));
     }
     // bins index of segment element q = col * D + ph: j = (jbase + q) mod M, M a
     // power of two (next_power_of_two, fft.cpp:80-82), so the wrap is a mask
@@ -106,19 +111,20 @@ __global__ void __launch_bounds__(256)
         const float2* r3 = r2 + sub;
         const int t_beg = __ldg(ph_off + ph), t_end = __ldg(ph_off + ph + 1);
         float2 w0 = r0[0], w1 = r1[0], w2 = r2[0], w3;
-        const float2* hp = tp + t_beg;
+        const float4* hp = tp4 + t_beg;
+        const float2* hg = taps_pm + t_beg;
         for (int t = 0, i = 0; t < t_end - t_beg; t += 4, i++) {
-            float2 h;
-            w3 = r3[i]; h = hp[t];
+            float4 h;
+            w3 = r3[i]; h = TAPS_SMEM ? hp[t] : tap4(__ldg(hg + t));
             if (PD) { cmac(y0, w0, h); cmac(y1, w1, h); cmac(y2, w2, h); cmac(y3, w3, h); }
             else { rmac(y0, w0, h); rmac(y1, w1, h); rmac(y2, w2, h); rmac(y3, w3, h); }
-            w0 = r0[i + 1]; h = hp[t + 1];
+            w0 = r0[i + 1]; h = TAPS_SMEM ? hp[t + 1] : tap4(__ldg(hg + t + 1));
             if (PD) { cmac(y0, w1, h); cmac(y1, w2, h); cmac(y2, w3, h); cmac(y3, w0, h); }
             else { rmac(y0, w1, h); rmac(y1, w2, h); rmac(y2, w3, h); rmac(y3, w0, h); }
-            w1 = r1[i + 1]; h = hp[t + 2];
+            w1 = r1[i + 1]; h = TAPS_SMEM ? hp[t + 2] : tap4(__ldg(hg + t + 2));
             if (PD) { cmac(y0, w2, h); cmac(y1, w3, h); cmac(y2, w0, h); cmac(y3, w1, h); }
             else { rmac(y0, w2, h); rmac(y1, w3, h); rmac(y2, w0, h); rmac(y3, w1, h); }
-            w2 = r2[i + 1]; h = hp[t + 3];
+            w2 = r2[i + 1]; h = TAPS_SMEM ? hp[t + 3] : tap4(__ldg(hg + t + 3));
             if (PD) { cmac(y0, w3, h); cmac(y1, w0, h); cmac(y2, w1, h); cmac(y3, w2, h); }
             else { rmac(y0, w3, h); rmac(y1, w0, h); rmac(y2, w1, h); rmac(y3, w2, h); }
         }
@@ -163,7 +169,8 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
     while (threads > 32 && (int64_t)num_lines * nblk < 2 * 152) threads = threads_for(++nblk);
     nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
     auto smem_for = [&](int th, int taps_smem) {
-        return ((size_t)4 * conv_sub(th, max_ph_taps) * decimation + (taps_smem ? (size_t)ntaps_pm : 0)) * sizeof(float2);
+        return (size_t)4 * conv_sub(th, max_ph_taps) * decimation * sizeof(float2) +
+               (taps_smem ? (size_t)ntaps_pm * sizeof(float4) : 0);
     };
     int taps_in_smem = 1;
     const size_t limit = 200 * 1024;
@@ -174,20 +181,16 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
     const int sub = conv_sub(threads, max_ph_taps), cols = conv_cols(threads, max_ph_taps);
     nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
     const dim3 grid((unsigned)nblk, (unsigned)num_lines);
-    if (phase_delay) {
-        auto k = convolve_demodulate_kernel<true>;
+    auto launch = [&](auto k) -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
-                                           nd, sub, cols, taps_in_smem, demod, out);
-    } else {
-        auto k = convolve_demodulate_kernel<false>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
-                                           nd, sub, cols, taps_in_smem, demod, out);
-    }
-    return cudaGetLastError();
+                                           nd, sub, cols, demod, out);
+        return cudaGetLastError();
+    };
+    if (phase_delay) return taps_in_smem ? launch(convolve_demodulate_kernel<true, true>)
+                                         : launch(convolve_demodulate_kernel<true, false>);
+    return taps_in_smem ? launch(convolve_demodulate_kernel<false, true>) : launch(convolve_demodulate_kernel<false, false>);
 }
 
 int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph) {

@@ -451,6 +451,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     extern __shared__ __align__(128) float4 sm[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ int s_lut_base, s_lut_planes;
+    // segments of the chunk: record index ranges [s_seg[k], s_seg[k+1]) within
+    // one bin and one fold group (the walk folds and stores only at their ends)
+    __shared__ int s_seg[1024 + 2];
+    __shared__ int s_seg_warp[32];
+    __shared__ int s_nseg;
     const int n_valid = __ldg(counts);
     const int64_t start = (int64_t)blockIdx.x * chunk;
     if (start >= n_valid) return;
@@ -511,6 +516,32 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     const float ce = 0.5f * (float)(b.ne - 2), he = 0.5f * (float)b.ne;
     const bool cull = !REF && p.cull;
     const int nwords = (cnt + 31) >> 5;
+    {
+        // a record starts a segment where its bin differs from its predecessor's
+        // or at a fold-group start; ordered compaction: a ballot per warp, then a
+        // scan of the warps' counts
+        const int nwarps = blockDim.x >> 5, wid = tid >> 5;
+        int total = 0;
+        for (int base = 0; base < cnt; base += blockDim.x) {
+            const int r = base + tid;
+            const bool start = r < cnt && (r == 0 || (r % FOLD) == 0 ||
+                                           __float_as_int(smB[r].w) != __float_as_int(smB[r - 1].w));
+            const unsigned bal = __ballot_sync(0xffffffffu, start);
+            if (lane == 0) s_seg_warp[wid] = __popc(bal);
+            __syncthreads();
+            int off = total;
+            for (int k = 0; k < wid; k++) off += s_seg_warp[k];
+            if (start) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = r;
+            for (int k = 0; k < nwarps; k++) total += s_seg_warp[k];
+            __syncthreads();
+        }
+        if (tid == 0) {
+            s_seg[total] = cnt;
+            s_nseg = total;
+        }
+        __syncthreads();
+    }
+    const int nseg = s_nseg;
 
     for (int g0 = 0; g0 < L; g0 += blockDim.x) {
         if (g0 + (tid & ~31) >= L) break;   // this warp has no line in this group (nor in later ones)
@@ -555,45 +586,24 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             }
         }
 
-        // ---- phase B: walk the selected records in bin order ----
+        // ---- phase B: walk the selected records, segment by segment ----
         // COUNT: pairs visited, pairs with a non-zero weight, walk steps in which
         // no lane of the warp had a non-zero weight
         unsigned walked = 0, weighted = 0, idle_steps = 0;
         int cur = first_bin;
         long long tr = 0, ti = 0;
-        float ar = 0.0f, ai = 0.0f;
-        // fold groups: FOLD records = FOLD/32 mask words; the chunk starts at a
-        // multiple of FOLD, so the FP32 run sums end at absolute record indices
-        // k*FOLD whatever the chunk size
-        for (int w0 = 0; w0 < nwords; w0 += FOLD / 32) {
-            const int w1 = min(w0 + FOLD / 32, nwords);
-            for (int w = w0; w < w1; w++) {
+        for (int sg = 0; sg < nseg; sg++) {
+            const int lo = s_seg[sg], hi = s_seg[sg + 1];
+            float ar = 0.0f, ai = 0.0f;
+            for (int w = lo >> 5; w <= (hi - 1) >> 5; w++) {
                 unsigned word = cull ? __shfl_sync(0xffffffffu, mask, w) : 0xffffffffu;
-                if (!cull && w == nwords - 1 && (cnt & 31)) word &= (1u << (cnt & 31)) - 1u;
+                // the segment's records of this word
+                if (w == (lo >> 5)) word &= 0xffffffffu << (lo & 31);
+                if (w == ((hi - 1) >> 5) && (hi & 31)) word &= (1u << (hi & 31)) - 1u;
                 while (word) {
                     const int i = (w << 5) + __ffs(word) - 1;
                     word &= word - 1u;
                     const float4 B = smB[i];
-                    const int idx = __float_as_int(B.w);
-                    if (idx != cur) {   // warp-uniform: the record is the same for all lanes
-                        tr += f2ll_rn(ar * scale);
-                        if (PD) ti += f2ll_rn(ai * scale);
-                        ar = 0.0f;
-                        ai = 0.0f;
-                        if (active) {
-                            unsigned long long* dst = lb + (int64_t)cur * stride;
-                            if (cur == first_bin || cur == last_bin) {
-                                if (tr) atomicAdd(dst, (unsigned long long)tr);
-                                if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
-                            } else {
-                                if (tr) dst[0] = (unsigned long long)tr;
-                                if (PD && ti) dst[1] = (unsigned long long)ti;
-                            }
-                        }
-                        tr = 0;
-                        ti = 0;
-                        cur = idx;
-                    }
                     const float4 A = smA[i];
                     float w8;
                     if (REF) {
@@ -666,10 +676,27 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     }
                 }
             }
+            // end of the segment: fold the FP32 run into the integer total; at a
+            // bin change store it (plain store inside the chunk, atomic at its
+            // edge bins: other CTAs hold records there)
             tr += f2ll_rn(ar * scale);
             if (PD) ti += f2ll_rn(ai * scale);
-            ar = 0.0f;
-            ai = 0.0f;
+            const int next = sg + 1 < nseg ? __float_as_int(smB[hi].w) : -1;
+            if (next != cur) {
+                if (active) {
+                    unsigned long long* dst = lb + (int64_t)cur * stride;
+                    if (cur == first_bin || cur == last_bin) {
+                        if (tr) atomicAdd(dst, (unsigned long long)tr);
+                        if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
+                    } else {
+                        if (tr) dst[0] = (unsigned long long)tr;
+                        if (PD && ti) dst[1] = (unsigned long long)ti;
+                    }
+                }
+                tr = 0;
+                ti = 0;
+                cur = next;
+            }
         }
         if (COUNT) {
             walked = __reduce_add_sync(0xffffffffu, walked);
@@ -678,16 +705,6 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 atomicAdd(pair_counts, (unsigned long long)walked);
                 atomicAdd(pair_counts + 1, (unsigned long long)weighted);
                 atomicAdd(pair_counts + 2, (unsigned long long)idle_steps);
-            }
-        }
-        if (active) {
-            unsigned long long* dst = lb + (int64_t)cur * stride;
-            if (cur == first_bin || cur == last_bin) {
-                if (tr) atomicAdd(dst, (unsigned long long)tr);
-                if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
-            } else {
-                if (tr) dst[0] = (unsigned long long)tr;
-                if (PD && ti) dst[1] = (unsigned long long)ti;
             }
         }
     }
