@@ -566,20 +566,22 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 bool pass = false;
                 if (r < cnt) {
                     const float4 A = smA[r];
-                    const int idx = __float_as_int(smB[r].w);
-                    // distance bound from the bin: rho*k <= idx + 1/2
-                    const float rho = ((float)idx + 0.5f) * p.cull_rho_per_bin;
                     const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
                     const float v = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
                     const float dt = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
-                    // |A_perp| = |A x r| (no cancellation for A along r), rounded up
+                    // |A_perp|^2 = |A x r|^2 (no cancellation for A along r); |A_perp|
+                    // bounded from above (rsqrt's error is far below 1e-5)
                     const float cx = fmaf(A.y, rz, -A.z * ry), cy = fmaf(A.z, rx, -A.x * rz);
                     const float cz = fmaf(A.x, ry, -A.y * rx);
-                    const float ap = __fsqrt_ru(fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
+                    const float ap2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+                    const float ap = ap2 * rsqrtf(fmaxf(ap2, 1e-30f)) * 1.00001f;
                     const float adt = fabsf(dt);
                     const float su = fmaf(adt, du_par, ap * du_perp), sv = fmaf(adt, dv_par, ap * dv_perp);
+                    // some line may have the record in front: A.r_k >= dt - |A| dd,
+                    // with |A|^2 = dt^2 + |A_perp|^2
+                    const bool front = dt >= 0.0f || fmaf(dt, dt, ap2) * (dd * dd) >= dt * dt;
                     pass = (u + su > p.cull_l_lo) && (u - su < p.cull_l_hi) && (v + sv > p.cull_e_lo) &&
-                           (v - sv < p.cull_e_hi) && (dt + rho * dd >= 0.0f);
+                           (v - sv < p.cull_e_hi) && front;
                 }
                 const unsigned m = __ballot_sync(0xffffffffu, pass);
                 if (lane == w) mask = m;
@@ -638,11 +640,15 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                                 // with the fraction dropped for -1 < t < 0
                                 // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
                                 // integer part of max(t, 0) + 2^23 rounded down
-                                const float uc = fmaxf(u, 0.0f), vc = fmaxf(v, 0.0f);
-                                const float tu = __fadd_rd(uc, 8388608.0f), tv = __fadd_rd(vc, 8388608.0f);
-                                const int l0 = __float_as_int(tu) - 0x4B000000, e0 = __float_as_int(tv) - 0x4B000000;
-                                const float fl = uc - (tu - 8388608.0f);
-                                const float fe = vc - (tv - 8388608.0f);
+                                // (paired FP32 operations, two per instruction; the same
+                                // rounding per component as the scalar forms)
+                                const float2 ucv = make_float2(fmaxf(u, 0.0f), fmaxf(v, 0.0f));
+                                const float2 t2 = __fadd2_rd(ucv, make_float2(8388608.0f, 8388608.0f));
+                                const int l0 = __float_as_int(t2.x) - 0x4B000000, e0 = __float_as_int(t2.y) - 0x4B000000;
+                                // fraction = t - floor(t): uc - (tu - 2^23), both differences exact
+                                const float2 fle = __ffma2_rn(__fadd2_rn(t2, make_float2(-8388608.0f, -8388608.0f)),
+                                                              make_float2(-1.0f, -1.0f), ucv);
+                                const float fl = fle.x, fe = fle.y;
                                 const int r0 = __float_as_int(B.z);
                                 float4 P, Q;
                                 if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
@@ -657,13 +663,13 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                                 const float fr = B.y;
                                 // radial (the table holds the radial differences),
                                 // lateral, elevational (BeamProfile.cpp:116-127)
-                                const float c00 = fmaf(fr, P.z, P.x);
-                                const float c01 = fmaf(fr, P.w, P.y);
-                                const float c10 = fmaf(fr, Q.z, Q.x);
-                                const float c11 = fmaf(fr, Q.w, Q.y);
-                                const float c0 = fmaf(fl, c10 - c00, c00);
-                                const float c1 = fmaf(fl, c11 - c01, c01);
-                                w8 = fmaf(fe, c1 - c0, c0);
+                                // (c00, c01) and (c10, c11), then (c0, c1) = c.0 + fl (c.1 - c.0)
+                                const float2 frr = make_float2(fr, fr);
+                                const float2 cl0 = __ffma2_rn(frr, make_float2(P.z, P.w), make_float2(P.x, P.y));
+                                const float2 cl1 = __ffma2_rn(frr, make_float2(Q.z, Q.w), make_float2(Q.x, Q.y));
+                                const float2 dl = __ffma2_rn(cl0, make_float2(-1.0f, -1.0f), cl1);
+                                const float2 ce2 = __ffma2_rn(make_float2(fl, fl), dl, cl0);
+                                w8 = fmaf(fe, ce2.y - ce2.x, ce2.x);
                             }
                         }
                     }
