@@ -588,122 +588,137 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             }
         }
 
-        // ---- phase B: walk the selected records, segment by segment ----
+        // ---- phase B: walk the selected records in order ----
+        // Only words with selected records are visited (lane w holds word w).  A
+        // record past the current segment's end closes it: its FP32 run is folded
+        // into the integer total, and at a bin change the total is stored (a
+        // plain store inside the chunk, an atomic at its edge bins: other CTAs
+        // hold records there).  Segments without a selected record cost nothing.
         // COUNT: pairs visited, pairs with a non-zero weight, walk steps in which
         // no lane of the warp had a non-zero weight
         unsigned walked = 0, weighted = 0, idle_steps = 0;
-        int cur = first_bin;
+        const unsigned mask_w = cull ? mask
+                                     : (lane < nwords ? ((lane == nwords - 1 && (cnt & 31)) ? (1u << (cnt & 31)) - 1u
+                                                                                            : 0xffffffffu)
+                                                      : 0u);
+        unsigned nz = __ballot_sync(0xffffffffu, mask_w != 0u);
+        int cur = first_bin, sg = 0, seg_end = s_seg[1];
         long long tr = 0, ti = 0;
-        for (int sg = 0; sg < nseg; sg++) {
-            const int lo = s_seg[sg], hi = s_seg[sg + 1];
-            float ar = 0.0f, ai = 0.0f;
-            for (int w = lo >> 5; w <= (hi - 1) >> 5; w++) {
-                unsigned word = cull ? __shfl_sync(0xffffffffu, mask, w) : 0xffffffffu;
-                // the segment's records of this word
-                if (w == (lo >> 5)) word &= 0xffffffffu << (lo & 31);
-                if (w == ((hi - 1) >> 5) && (hi & 31)) word &= (1u << (hi & 31)) - 1u;
-                while (word) {
-                    const int i = (w << 5) + __ffs(word) - 1;
-                    word &= word - 1u;
-                    const float4 B = smB[i];
-                    const float4 A = smA[i];
-                    float w8;
-                    if (REF) {
-                        // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
-                        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
-                        const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
-                        const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
-                        if (BEAM == BEAM_GAUSSIAN) {
-                            w8 = gauss_weight_ref(b, l, e);
-                        } else {
-                            // the reference recomputes the radial table coordinate per pair from r
-                            w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
-                                                                       __fmul_rn(A.z, A.z))),
-                                                l, e);
-                        }
+        float ar = 0.0f, ai = 0.0f;
+        auto store_bin = [&]() {
+            if (active) {
+                unsigned long long* dst = lb + (int64_t)cur * stride;
+                if (cur == first_bin || cur == last_bin) {
+                    if (tr) atomicAdd(dst, (unsigned long long)tr);
+                    if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
+                } else {
+                    if (tr) dst[0] = (unsigned long long)tr;
+                    if (PD && ti) dst[1] = (unsigned long long)ti;
+                }
+            }
+        };
+        while (nz) {
+            const int w = __ffs(nz) - 1;
+            nz &= nz - 1u;
+            unsigned word = __shfl_sync(0xffffffffu, mask_w, w);
+            while (word) {
+                const int i = (w << 5) + __ffs(word) - 1;
+                word &= word - 1u;
+                const float4 B = smB[i];
+                const float4 A = smA[i];
+                if (i >= seg_end) {   // warp-uniform
+                    tr += f2ll_rn(ar * scale);
+                    if (PD) ti += f2ll_rn(ai * scale);
+                    ar = 0.0f;
+                    ai = 0.0f;
+                    do { sg++; } while (s_seg[sg + 1] <= i);
+                    seg_end = s_seg[sg + 1];
+                    const int nb = __float_as_int(B.w);
+                    if (nb != cur) {
+                        store_bin();
+                        tr = 0;
+                        ti = 0;
+                        cur = nb;
+                    }
+                }
+                float w8;
+                if (REF) {
+                    // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
+                    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
+                    const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
+                    const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
+                    if (BEAM == BEAM_GAUSSIAN) {
+                        w8 = gauss_weight_ref(b, l, e);
+                    } else {
+                        // the reference recomputes the radial table coordinate per pair from r
+                        w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                                   __fmul_rn(A.z, A.z))),
+                                            l, e);
+                    }
+                    w8 = signbit(dot) ? 0.0f : w8;
+                } else {
+                    const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
+                    const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
+                    const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
+                    if (BEAM == BEAM_GAUSSIAN) {
+                        w8 = exp2f(-fmaf(u, u, v * v));
+                        // arc projection: a line for which the scatterer lies behind the
+                        // origin sees it at -rho, outside [0, ns) for every record
+                        // (near-origin scatterers take the per-pair path)
                         w8 = signbit(dot) ? 0.0f : w8;
                     } else {
-                        const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
-                        const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
-                        const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
-                        if (BEAM == BEAM_GAUSSIAN) {
-                            w8 = exp2f(-fmaf(u, u, v * v));
-                            // arc projection: a line for which the scatterer lies behind the
-                            // origin sees it at -rho, outside [0, ns) for every record
-                            // (near-origin scatterers take the per-pair path)
-                            w8 = signbit(dot) ? 0.0f : w8;
-                        } else {
-                            w8 = 0.0f;
-                            // (a warp whose lanes all miss the table skips the lookup)
-                            if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
-                                // -1 < t < n-1: the reference's trunc-toward-zero index
-                                // with the fraction dropped for -1 < t < 0
-                                // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
-                                // integer part of max(t, 0) + 2^23 rounded down
-                                // (paired FP32 operations, two per instruction; the same
-                                // rounding per component as the scalar forms)
-                                const float2 ucv = make_float2(fmaxf(u, 0.0f), fmaxf(v, 0.0f));
-                                const float2 t2 = __fadd2_rd(ucv, make_float2(8388608.0f, 8388608.0f));
-                                const int l0 = __float_as_int(t2.x) - 0x4B000000, e0 = __float_as_int(t2.y) - 0x4B000000;
-                                // fraction = t - floor(t): uc - (tu - 2^23), both differences exact
-                                const float2 fle = __ffma2_rn(__fadd2_rn(t2, make_float2(-8388608.0f, -8388608.0f)),
-                                                              make_float2(-1.0f, -1.0f), ucv);
-                                const float fl = fle.x, fe = fle.y;
-                                const int r0 = __float_as_int(B.z);
-                                float4 P, Q;
-                                if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
-                                    const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
-                                    P = pl[0];
-                                    Q = pl[lut_row];
-                                } else {
-                                    const int base = r0 * lut_plane_size + l0 * b.ne + e0;
-                                    P = __ldg(b.lut4 + base);
-                                    Q = __ldg(b.lut4 + base + b.ne);
-                                }
-                                const float fr = B.y;
-                                // radial (the table holds the radial differences),
-                                // lateral, elevational (BeamProfile.cpp:116-127)
-                                // (c00, c01) and (c10, c11), then (c0, c1) = c.0 + fl (c.1 - c.0)
-                                const float2 frr = make_float2(fr, fr);
-                                const float2 cl0 = __ffma2_rn(frr, make_float2(P.z, P.w), make_float2(P.x, P.y));
-                                const float2 cl1 = __ffma2_rn(frr, make_float2(Q.z, Q.w), make_float2(Q.x, Q.y));
-                                const float2 dl = __ffma2_rn(cl0, make_float2(-1.0f, -1.0f), cl1);
-                                const float2 ce2 = __ffma2_rn(make_float2(fl, fl), dl, cl0);
-                                w8 = fmaf(fe, ce2.y - ce2.x, ce2.x);
+                        w8 = 0.0f;
+                        // (a warp whose lanes all miss the table skips the lookup)
+                        if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
+                            // -1 < t < n-1: the reference's trunc-toward-zero index
+                            // with the fraction dropped for -1 < t < 0
+                            // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
+                            // integer part of max(t, 0) + 2^23 rounded down
+                            // (paired FP32 operations, two per instruction; the same
+                            // rounding per component as the scalar forms)
+                            const float2 ucv = make_float2(fmaxf(u, 0.0f), fmaxf(v, 0.0f));
+                            const float2 t2 = __fadd2_rd(ucv, make_float2(8388608.0f, 8388608.0f));
+                            const int l0 = __float_as_int(t2.x) - 0x4B000000, e0 = __float_as_int(t2.y) - 0x4B000000;
+                            // fraction = t - floor(t): uc - (tu - 2^23), both differences exact
+                            const float2 fle = __ffma2_rn(__fadd2_rn(t2, make_float2(-8388608.0f, -8388608.0f)),
+                                                          make_float2(-1.0f, -1.0f), ucv);
+                            const float fl = fle.x, fe = fle.y;
+                            const int r0 = __float_as_int(B.z);
+                            float4 P, Q;
+                            if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
+                                const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
+                                P = pl[0];
+                                Q = pl[lut_row];
+                            } else {
+                                const int base = r0 * lut_plane_size + l0 * b.ne + e0;
+                                P = __ldg(b.lut4 + base);
+                                Q = __ldg(b.lut4 + base + b.ne);
                             }
+                            const float fr = B.y;
+                            // radial (the table holds the radial differences),
+                            // lateral, elevational (BeamProfile.cpp:116-127)
+                            // (c00, c01) and (c10, c11), then (c0, c1) = c.0 + fl (c.1 - c.0)
+                            const float2 frr = make_float2(fr, fr);
+                            const float2 cl0 = __ffma2_rn(frr, make_float2(P.z, P.w), make_float2(P.x, P.y));
+                            const float2 cl1 = __ffma2_rn(frr, make_float2(Q.z, Q.w), make_float2(Q.x, Q.y));
+                            const float2 dl = __ffma2_rn(cl0, make_float2(-1.0f, -1.0f), cl1);
+                            const float2 ce2 = __ffma2_rn(make_float2(fl, fl), dl, cl0);
+                            w8 = fmaf(fe, ce2.y - ce2.x, ce2.x);
                         }
                     }
-                    ar = fmaf(w8, A.w, ar);
-                    if (PD) ai = fmaf(w8, B.x, ai);
-                    if (COUNT) {
-                        walked += active ? 1u : 0u;
-                        weighted += (active && w8 != 0.0f) ? 1u : 0u;
-                        idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
-                    }
                 }
-            }
-            // end of the segment: fold the FP32 run into the integer total; at a
-            // bin change store it (plain store inside the chunk, atomic at its
-            // edge bins: other CTAs hold records there)
-            tr += f2ll_rn(ar * scale);
-            if (PD) ti += f2ll_rn(ai * scale);
-            const int next = sg + 1 < nseg ? __float_as_int(smB[hi].w) : -1;
-            if (next != cur) {
-                if (active) {
-                    unsigned long long* dst = lb + (int64_t)cur * stride;
-                    if (cur == first_bin || cur == last_bin) {
-                        if (tr) atomicAdd(dst, (unsigned long long)tr);
-                        if (PD && ti) atomicAdd(dst + 1, (unsigned long long)ti);
-                    } else {
-                        if (tr) dst[0] = (unsigned long long)tr;
-                        if (PD && ti) dst[1] = (unsigned long long)ti;
-                    }
+                ar = fmaf(w8, A.w, ar);
+                if (PD) ai = fmaf(w8, B.x, ai);
+                if (COUNT) {
+                    walked += active ? 1u : 0u;
+                    weighted += (active && w8 != 0.0f) ? 1u : 0u;
+                    idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
                 }
-                tr = 0;
-                ti = 0;
-                cur = next;
             }
         }
+        tr += f2ll_rn(ar * scale);
+        if (PD) ti += f2ll_rn(ai * scale);
+        store_bin();
         if (COUNT) {
             walked = __reduce_add_sync(0xffffffffu, walked);
             weighted = __reduce_add_sync(0xffffffffu, weighted);
