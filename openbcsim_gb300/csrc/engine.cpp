@@ -138,6 +138,7 @@ cudaStream_t Simulator::stream() {
 void Simulator::set_parameter(const std::string& key, const std::string& value) {
     bool b = false;
     cfg_version_++;
+    static_version_++;
     if (key == "verbose") {
         verbose_ = std::stoi(value);
     } else if (key == "sound_speed") {
@@ -256,6 +257,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
 // ---------------------------------------------------------------------------
 void Simulator::set_excitation(const float* samples, int n, int center_index, float fs, float demod_freq) {
     cfg_version_++;
+    static_version_++;
     if (n < 0 || (n > 0 && !samples)) throw SimError(BCSIM_E_INVALID, "set_excitation: invalid samples");
     taps_.assign(samples, samples + n);
     center_ = center_index;
@@ -307,6 +309,7 @@ void Simulator::set_scan_sequence(const float* origins, const float* dirs, const
     lines_valid_ = false;
     tables_valid_ = false;
     cfg_version_++;
+    static_version_++;
 }
 
 void Simulator::copy_scan_from(const Simulator& o) {
@@ -322,10 +325,12 @@ void Simulator::copy_scan_from(const Simulator& o) {
     lines_valid_ = false;
     tables_valid_ = false;
     cfg_version_++;
+    static_version_++;
 }
 
 void Simulator::set_analytical_profile(float sigma_lateral, float sigma_elevational) {
     cfg_version_++;
+    static_version_++;
     log(1, "Setting analytical beam profile for GPU algorithm");
     beam_type_ = BEAM_GAUSSIAN;
     sigma_l_ = sigma_lateral;
@@ -349,6 +354,7 @@ void Simulator::set_lookup_profile(const float* samples, int nr, int nl, int ne,
     beam_type_ = BEAM_LUT;
     lut_uploaded_ = false;
     cfg_version_++;
+    static_version_++;
 }
 
 void Simulator::clear_fixed_scatterers() {
@@ -714,11 +720,57 @@ struct EventTimer {
 // ---------------------------------------------------------------------------
 // prepare: everything the host computes or uploads for one configuration
 // ---------------------------------------------------------------------------
+// Fixed-point scale 2^S of the bins: S = floor(61 - log2(sum |a| * max weight)),
+// so that no sum of contributions can overflow int64.
+void Simulator::set_fixed_point_scale(SimParams& p) const {
+    const double bound = fixed_point_bound();
+    int S = 0;
+    if (bound > 0.0 && std::isfinite(bound)) S = (int)std::floor(61.0 - std::log2(bound * 1.001));
+    S = std::max(-100, std::min(100, S));
+    p.log2scale = S;
+    p.scale = std::ldexp(1.0f, S);
+}
+
+// What the sorted shared-origin records depend on: the scatterers (by version),
+// the origin, the common time and the kernel constants.
+uint64_t Simulator::records_key_of(const Plan& P) const {
+    uint64_t key = data_version_ * 1000003ull;
+    auto mix = [&](const void* ptr, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(ptr);
+        for (size_t i = 0; i < n; i++) key = (key ^ c[i]) * 1099511628211ull;
+    };
+    mix(lines_[0].o, sizeof(lines_[0].o));
+    mix(&timestamps_[0], sizeof(float));
+    mix(&P.p, sizeof(P.p));
+    mix(&P.b, sizeof(P.b));
+    return key;
+}
+
+// The shapes a plan depends on: dataset sizes and spline knots (not the values).
+std::vector<double> Simulator::data_shape() const {
+    std::vector<double> v{(double)fixed_n_};
+    for (const auto& d : splines_) {
+        v.push_back((double)d.n);
+        v.push_back((double)d.num_cs);
+        v.push_back((double)d.degree);
+        for (float k : d.knots) v.push_back((double)k);
+    }
+    return v;
+}
+
 void Simulator::prepare() {
     throw_if_not_configured();
     if (amplitude_nonfinite_) throw SimError(BCSIM_E_INVALID, "Nan in scatterer projection.");
     ensure_device();
     if (plan_.version == cfg_version_) return;
+    if (plan_.version != ~0ull && plan_.static_version == static_version_ && plan_.data_shape == data_shape()) {
+        // only scatterer values changed (a new frame of the same phantom shape):
+        // the plan stands but for the fixed-point scale and the records' identity
+        set_fixed_point_scale(plan_.p);
+        if (plan_.n_shared > 0) plan_.records_key = records_key_of(plan_);
+        plan_.version = cfg_version_;
+        return;
+    }
     const cudaStream_t st = stream_;
     const int L = num_lines_;
     if (ns_ <= 0) throw SimError(BCSIM_E_INVALID, "line length gives no RF samples");
@@ -781,12 +833,7 @@ void Simulator::prepare() {
     p.k_hi = (float)k;
     p.k_lo = (float)(k - (double)p.k_hi);
     p.two_pi_fd_over_fs = (float)(6.283185307179586 * (double)fd_ / (double)fs_);
-    const double bound = fixed_point_bound();
-    int S = 0;
-    if (bound > 0.0 && std::isfinite(bound)) S = (int)std::floor(61.0 - std::log2(bound * 1.001));
-    S = std::max(-100, std::min(100, S));
-    p.log2scale = S;
-    p.scale = std::ldexp(1.0f, S);
+    set_fixed_point_scale(p);
     p.wide_cta = wide_cta_ ? 1 : 0;
     p.lut_smem = lut_smem_ ? 1 : 0;
     // exact culling ranges (fp64 mode): outside them the weight is exactly 0
@@ -967,21 +1014,13 @@ void Simulator::prepare() {
         int chunk = 1024;
         while (chunk > 128 && (N + chunk - 1) / chunk < 4 * 152) chunk /= 2;
         P.chunk = chunk;
-        // what the records depend on: scatterers, origin, common time, constants
-        uint64_t key = data_version_ * 1000003ull;
-        auto mix = [&](const void* ptr, size_t n) {
-            const unsigned char* c = static_cast<const unsigned char*>(ptr);
-            for (size_t i = 0; i < n; i++) key = (key ^ c[i]) * 1099511628211ull;
-        };
-        mix(lines_[0].o, sizeof(lines_[0].o));
-        mix(&timestamps_[0], sizeof(float));
-        mix(&p, sizeof(p));
-        mix(&b, sizeof(b));
-        P.records_key = key;
+        P.records_key = records_key_of(P);
     }
     // the host vectors above are pageable: finish their copies before they go
     BCSIM_CUDA(cudaStreamSynchronize(st));
     P.version = cfg_version_;
+    P.static_version = static_version_;
+    P.data_shape = data_shape();
     if (autotune_) autotune();
 }
 
@@ -1115,9 +1154,12 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     if (host_out) {
         EventTimer timer(store_details_, st);
         BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)num_lines_ * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
+        // the bounded-wait error flag travels with the result (one synchronisation)
+        if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
+        BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, st));
         BCSIM_CUDA(cudaStreamSynchronize(st));
         if (store_details_) debug_["kernel_memcpy_ms"].push_back(timer.stop());
-        check_device_flag();
+        if (*flag_host_.p) check_device_flag();   // clears the flag and reports
     }
 }
 
@@ -1269,6 +1311,7 @@ void Simulator::clone_from(Simulator& o) {
     tables_valid_ = false;
     lines_valid_ = false;
     cfg_version_++;
+    static_version_++;
     data_version_++;
 }
 

@@ -54,6 +54,17 @@ private:
     cudaStream_t stream_ = nullptr;   // stream-ordered allocation on this stream (null: cudaMalloc)
 };
 
+// Pinned host int (the error flag's landing place), freed with its owner.
+struct PinnedInt {
+    int* p = nullptr;
+    PinnedInt() = default;
+    PinnedInt(const PinnedInt&) = delete;
+    PinnedInt& operator=(const PinnedInt&) = delete;
+    ~PinnedInt() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 // A simulator's stream, destroyed (after its work) when the simulator goes --
 // declared before the simulator's buffers, so that those are freed first, in
 // its order.
@@ -94,6 +105,8 @@ struct GenLaunch {
 // prepare() and reused until the configuration changes.
 struct Plan {
     uint64_t version = ~0ull;
+    uint64_t static_version = ~0ull;   // configuration apart from scatterer values
+    std::vector<double> data_shape;    // dataset sizes and spline knots it was built for
     SimParams p;
     BeamDev b;
     bool shared = false;
@@ -168,11 +181,15 @@ private:
     void prepare_lines();
     void autotune();
     double fixed_point_bound() const;
+    void set_fixed_point_scale(SimParams& p) const;
+    uint64_t records_key_of(const Plan& P) const;
+    std::vector<double> data_shape() const;
 
     // configuration
     int device_ = 0;
     bool device_ready_ = false;
     OwnedStream owned_stream_;
+    PinnedInt flag_host_;
     cudaStream_t stream_ = nullptr;   // owned_stream_.s
     int verbose_ = 0;
     float sound_speed_ = 1540.0f;
@@ -196,6 +213,7 @@ private:
     DeviceBuffer pair_counts_;
     DeviceBuffer ingest_scratch_;   // amplitude reductions of add_*_scatterers
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
+    uint64_t static_version_ = 1;   // bumped by every change but new scatterer values
     uint64_t data_version_ = 1;  // bumped by every scatterer change
     uint64_t records_key_ = 0;
     Plan plan_;

@@ -185,4 +185,6 @@ cudaError_t abs_sum(const float* vals, int64_t stride, int64_t n, void* scratch,
                     cudaStream_t stream);
 
 cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream);
+// Copy of the error flag into host memory (pinned: asynchronous), in stream order.
+cudaError_t enqueue_error_flag_read(int* host_flag, cudaStream_t stream);
 }

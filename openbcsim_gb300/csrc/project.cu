@@ -1149,6 +1149,10 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
 #undef BCSIM_GEN
 }
 
+cudaError_t enqueue_error_flag_read(int* host_flag, cudaStream_t stream) {
+    return cudaMemcpyFromSymbolAsync(host_flag, g_bcsim_error_flag, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+}
+
 cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream) {
     cudaError_t e = cudaMemcpyFromSymbolAsync(flag, g_bcsim_error_flag, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
     if (e != cudaSuccess) return e;
