@@ -577,6 +577,59 @@ void bisect_lines(const std::vector<LineGeom>& lines, int* idx, int n) {
 }
 }  // namespace
 
+// Culling extent of a per-pair tile (lines ids[0 .. count)): its line nearest
+// the tiles' mean direction as reference, the frame spread about it (split along
+// and across its direction, as for the shared-origin slots) and the largest
+// origin offset, with margins for the float arithmetic of the test.
+static TileBox make_tile_box(const std::vector<LineGeom>& lines, const int* ids, int count) {
+    double m[3] = {0, 0, 0};
+    for (int i = 0; i < count; i++)
+        for (int k = 0; k < 3; k++) m[k] += lines[ids[i]].d[k];
+    const double mn = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+    int best = ids[0];
+    double best_dot = -2.0;
+    for (int i = 0; i < count; i++) {
+        const float* d = lines[ids[i]].d;
+        const double dot = mn > 0 ? (d[0] * m[0] + d[1] * m[1] + d[2] * m[2]) / mn : 0.0;
+        if (dot > best_dot) { best_dot = dot; best = ids[i]; }
+    }
+    const LineGeom& ref = lines[best];
+    double upar = 0, uperp = 0, vpar = 0, vperp = 0, dorig = 0;
+    for (int i = 0; i < count; i++) {
+        const LineGeom& g = lines[ids[i]];
+        double dl[3], de[3], pl = 0, pe = 0, oo = 0;
+        for (int k = 0; k < 3; k++) {
+            dl[k] = (double)g.l[k] - ref.l[k];
+            de[k] = (double)g.e[k] - ref.e[k];
+            pl += dl[k] * ref.d[k];
+            pe += de[k] * ref.d[k];
+            oo += ((double)g.o[k] - ref.o[k]) * ((double)g.o[k] - ref.o[k]);
+        }
+        double ql = 0, qe = 0;
+        for (int k = 0; k < 3; k++) {
+            const double xl = dl[k] - pl * ref.d[k], xe = de[k] - pe * ref.d[k];
+            ql += xl * xl;
+            qe += xe * xe;
+        }
+        upar = std::max(upar, std::fabs(pl));
+        uperp = std::max(uperp, std::sqrt(ql));
+        vpar = std::max(vpar, std::fabs(pe));
+        vperp = std::max(vperp, std::sqrt(qe));
+        dorig = std::max(dorig, std::sqrt(oo));
+    }
+    TileBox t;
+    t.ox = ref.o[0]; t.oy = ref.o[1]; t.oz = ref.o[2];
+    t.lx = ref.l[0]; t.ly = ref.l[1]; t.lz = ref.l[2];
+    t.ex = ref.e[0]; t.ey = ref.e[1]; t.ez = ref.e[2];
+    t.rx = ref.d[0]; t.ry = ref.d[1]; t.rz = ref.d[2];
+    t.du_par = (float)(upar * 1.0001 + 2e-6);
+    t.du_perp = (float)(uperp * 1.0001 + 2e-6);
+    t.dv_par = (float)(vpar * 1.0001 + 2e-6);
+    t.dv_perp = (float)(vperp * 1.0001 + 2e-6);
+    t.d_orig = (float)(dorig * 1.0001 + 1e-7);
+    return t;
+}
+
 static void order_lines(const std::vector<LineGeom>& lines, std::vector<int>& order, std::vector<SlotCone>& cones) {
     const int L = (int)lines.size();
     order.resize(L);
@@ -931,8 +984,10 @@ void Simulator::prepare() {
         }
     };
     std::vector<LineTile> all_tiles;
+    std::vector<TileBox> all_boxes;
     std::vector<int> all_ids;
     std::vector<LineBasis> all_basis;
+    P.tile_cull = mode_ == MODE_FP64 && cull_ && P.p.cull;
     auto add_gen = [&](int kind, int d) {
         std::vector<int> ids;
         std::vector<LineTile> tiles;
@@ -944,6 +999,8 @@ void Simulator::prepare() {
         g.num_tiles = tiles.size();
         g.basis_off = all_basis.size();
         const size_t id_off = all_ids.size();
+        if (P.tile_cull)
+            for (auto& t : tiles) all_boxes.push_back(make_tile_box(lines_, ids.data() + t.first, t.count));
         for (auto& t : tiles) t.first += (int)id_off;
         all_tiles.insert(all_tiles.end(), tiles.begin(), tiles.end());
         all_ids.insert(all_ids.end(), ids.begin(), ids.end());
@@ -962,6 +1019,9 @@ void Simulator::prepare() {
         BCSIM_CUDA(cudaMemcpyAsync(gen_line_ids_.get(), all_ids.data(), all_ids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!all_basis.empty())
         BCSIM_CUDA(cudaMemcpyAsync(gen_basis_.get(), all_basis.data(), all_basis.size() * sizeof(LineBasis), cudaMemcpyHostToDevice, st));
+    gen_boxes_.reserve(std::max<size_t>(1, all_boxes.size()) * sizeof(TileBox), stream_);
+    if (!all_boxes.empty())
+        BCSIM_CUDA(cudaMemcpyAsync(gen_boxes_.get(), all_boxes.data(), all_boxes.size() * sizeof(TileBox), cudaMemcpyHostToDevice, st));
 
     // device buffers
     const int stride = phase_delay_ ? 2 : 1;
@@ -1088,7 +1148,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
                                                   vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
-                                                  (int)g.num_tiles, nullptr, p, b, bins, st));
+                                                  (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
             } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
                 ++launches;
@@ -1096,7 +1156,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                                                   ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
-                                                  gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
+                                                  gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
             }
         }
         if (timing) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
@@ -1111,7 +1171,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
-                                              b, bins, st));
+                                              b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
         } else {
             if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
@@ -1119,7 +1179,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
-                                              gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st));
+                                              gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
         }
     }
     if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());

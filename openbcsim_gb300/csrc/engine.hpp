@@ -115,6 +115,7 @@ struct Plan {
     std::vector<int64_t> spline_off;
     std::vector<int> spline_first_cs;
     std::vector<GenLaunch> gl;
+    bool tile_cull = false;   // per-pair tiles carry culling boxes
     size_t bins_bytes = 0;
     size_t sort_tmp_bytes = 0;
     int end_bit = 1;
@@ -211,7 +212,8 @@ private:
     bool count_pairs_ = false;   // instrumented shared-origin kernel: visited / non-zero (record, line) pairs
     int last_launches_ = 0;      // kernels of this library launched by the last enqueue
     DeviceBuffer pair_counts_;
-    DeviceBuffer ingest_scratch_;   // amplitude reductions of add_*_scatterers
+    DeviceBuffer ingest_scratch_;
+    DeviceBuffer gen_boxes_;        // TileBox per per-pair tile   // amplitude reductions of add_*_scatterers
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
     uint64_t static_version_ = 1;   // bumped by every change but new scatterer values
     uint64_t data_version_ = 1;  // bumped by every scatterer change

@@ -81,6 +81,15 @@ struct LineTile {
     int span;   // control points staged per scatterer
 };
 
+// Extent of a per-pair line tile for culling: a reference line (origin o,
+// frame l, e, r), the frame spread of the tile's lines about it (as in
+// SlotCone) and the largest distance of a tile line's origin from o.
+struct TileBox {
+    float ox, oy, oz;
+    float lx, ly, lz, ex, ey, ez, rx, ry, rz;
+    float du_par, du_perp, dv_par, dv_perp, d_orig;
+};
+
 // Lines per CTA of the per-pair kernel (the largest line tile).
 constexpr int PAIR_THREADS = 128;
 
@@ -140,13 +149,15 @@ cudaError_t launch_project_shared(const float4* records, int64_t plane, const in
 // lines.  If index_list is given, the entries index_list[counts[0] ...
 // counts[0]+counts[1]) that fall in [list_lo, list_lo + n) are projected, as
 // scatterer (entry - list_lo) -- the near-origin residue of the shared path;
-// otherwise scatterers [0, n).
+// otherwise scatterers [0, n).  With boxes (one per tile, fp64 mode with exact
+// culling), a scatterer that no line of a tile can see with a contribution
+// that survives the fixed-point rounding is left out of that tile.
 cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const float* amps, int64_t n,
                                    int num_cs, int degree, const uint32_t* index_list, const int* counts,
                                    int64_t list_lo,
                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles,
                                    int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
-                                   unsigned long long* bins, cudaStream_t stream);
+                                   unsigned long long* bins, cudaStream_t stream, const TileBox* boxes = nullptr);
 
 // Fused convolution with the analytic pulse (direct FIR over a tap window),
 // IQ demodulation and radial decimation, from fixed-point bins to complex64.

@@ -785,9 +785,11 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                            const uint32_t* __restrict__ index_list, const int* __restrict__ counts,
                            int64_t list_lo, const LineGeom* __restrict__ lines, const int* __restrict__ line_ids,
                            const LineTile* __restrict__ tiles, const LineBasis* __restrict__ basis,
-                           unsigned long long* __restrict__ bins, SimParams p, BeamDev b) {
+                           unsigned long long* __restrict__ bins, SimParams p, BeamDev b,
+                           const TileBox* __restrict__ boxes) {
     __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? MAX_SPLINE_DEGREE + 1 : 1)];
     __shared__ float sa[PAIR_CHUNK];
+    __shared__ int s_kept;   // scatterers of the chunk kept for the tile
     const LineTile tile = tiles[blockIdx.y];
     int64_t count = n, list_off = 0;
     if (index_list) {
@@ -824,28 +826,94 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const float skip_below = 0.499f / p.scale;
     const float gl = b.gl, ge = b.ge;
 
+    // tile culling: the tile's reference frame and spreads
+    const bool tcull = boxes != nullptr;
+    TileBox bx;
+    if (tcull) bx = boxes[blockIdx.y];
+    const int lane = tid & 31;
+
     for (int64_t c0 = (int64_t)blockIdx.x * chunk; c0 < count; c0 += (int64_t)gridDim.x * chunk) {
-    const int cnt = (int)min((int64_t)chunk, count - c0);
+    const int cand = (int)min((int64_t)chunk, count - c0);
     __syncthreads();   // the previous chunk is consumed
-    // stage the chunk (gathering through the index list for the near-origin residue)
-    for (int i = tid; i < cnt; i += blockDim.x) {
-        int64_t s = c0 + i;
-        bool ok = true;
-        if (index_list) {
+    if (tid == 0) s_kept = 0;
+    __syncthreads();
+    // stage the chunk's scatterers that the tile may see (gathering through the
+    // index list for the near-origin residue), compacted: the order does not
+    // matter, every contribution is an integer atomic
+    for (int i0 = 0; i0 < cand; i0 += blockDim.x) {
+        const int ci = i0 + tid;
+        int64_t s = c0 + ci;
+        bool ok = ci < cand;
+        if (ok && index_list) {
             s = (int64_t)__ldg(index_list + list_off + s) - list_lo;
             ok = s >= 0 && s < n;
         }
-        if (SPLINE) {
-            for (int k = 0; k < span; k++)
-                sp[i * span + k] = ok ? __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-            sa[i] = ok ? __ldg(amps + s) : 0.0f;
-        } else {
-            const float4 q = ok ? __ldg(xyza + s) : make_float4(0.f, 0.f, 0.f, 0.f);
-            sp[i] = q;
-            sa[i] = ok ? q.w : 0.0f;
+        float a = 0.0f;
+        float lo_x = 0.f, lo_y = 0.f, lo_z = 0.f, hi_x = 0.f, hi_y = 0.f, hi_z = 0.f;
+        if (ok) {
+            if (SPLINE) {
+                a = __ldg(amps + s);
+                // convex hull: the curve over the tile's knot intervals lies in the
+                // box of the window's control points
+                lo_x = lo_y = lo_z = INFINITY;
+                hi_x = hi_y = hi_z = -INFINITY;
+                for (int k = 0; k < span; k++) {
+                    const float4 c = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+                    lo_x = fminf(lo_x, c.x); lo_y = fminf(lo_y, c.y); lo_z = fminf(lo_z, c.z);
+                    hi_x = fmaxf(hi_x, c.x); hi_y = fmaxf(hi_y, c.y); hi_z = fmaxf(hi_z, c.z);
+                }
+            } else {
+                const float4 q = __ldg(xyza + s);
+                a = q.w;
+                lo_x = hi_x = q.x; lo_y = hi_y = q.y; lo_z = hi_z = q.z;
+            }
+            ok = a != 0.0f;
+        }
+        if (ok && tcull) {
+            // lateral / elevational ranges outside which no contribution survives:
+            // the lookup table's extent, or (Gaussian) where w |a| <= 1/4 of a
+            // fixed-point unit, i.e. l^2 gl + e^2 ge >= log2(scale |a|) + 2
+            float llo = p.cull_l_lo, lhi = p.cull_l_hi, elo = p.cull_e_lo, ehi = p.cull_e_hi;
+            if (BEAM == BEAM_GAUSSIAN) {
+                const float Q = log2f(p.scale * fabsf(a)) + 2.01f;
+                const float rl = Q > 0.0f ? sqrtf(Q / gl) : 0.0f, re = Q > 0.0f ? sqrtf(Q / ge) : 0.0f;
+                llo = -rl; lhi = rl; elo = -re; ehi = re;
+                ok = Q > 0.0f;
+            }
+            const float cx = 0.5f * (lo_x + hi_x) - bx.ox, cy = 0.5f * (lo_y + hi_y) - bx.oy;
+            const float cz = 0.5f * (lo_z + hi_z) - bx.oz;
+            const float hx = 0.5f * (hi_x - lo_x) * 1.0001f, hy = 0.5f * (hi_y - lo_y) * 1.0001f;
+            const float hz = 0.5f * (hi_z - lo_z) * 1.0001f;
+            const float uc = fmaf(cz, bx.lz, fmaf(cy, bx.ly, cx * bx.lx));
+            const float uh = fmaf(hz, fabsf(bx.lz), fmaf(hy, fabsf(bx.ly), hx * fabsf(bx.lx))) + 1e-6f;
+            const float vc = fmaf(cz, bx.ez, fmaf(cy, bx.ey, cx * bx.ex));
+            const float vh = fmaf(hz, fabsf(bx.ez), fmaf(hy, fabsf(bx.ey), hx * fabsf(bx.ex))) + 1e-6f;
+            const float dc = fmaf(cz, bx.rz, fmaf(cy, bx.ry, cx * bx.rx));
+            const float dh = fmaf(hz, fabsf(bx.rz), fmaf(hy, fabsf(bx.ry), hx * fabsf(bx.rx))) + 1e-6f;
+            const float amax = fabsf(cx) + fabsf(cy) + fabsf(cz) + hx + hy + hz;   // >= |A - o|
+            const float adt = fabsf(dc) + dh;
+            // a tile line's coordinates differ from the reference's by the frame
+            // spread times the offset, plus its origin's distance from o
+            const float su = (fmaf(adt, bx.du_par, amax * bx.du_perp) + bx.d_orig) * 1.001f + 1e-6f;
+            const float sv = (fmaf(adt, bx.dv_par, amax * bx.dv_perp) + bx.d_orig) * 1.001f + 1e-6f;
+            ok = ok && (uc + uh + su > llo) && (uc - uh - su < lhi) && (vc + vh + sv > elo) && (vc - vh - sv < ehi);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        int base = 0;
+        if (lane == 0 && bal) base = atomicAdd(&s_kept, __popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (ok) {
+            const int d = base + __popc(bal & ((1u << lane) - 1u));
+            if (SPLINE) {
+                for (int k = 0; k < span; k++) sp[d * span + k] = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+            } else {
+                sp[d] = make_float4(lo_x, lo_y, lo_z, a);
+            }
+            sa[d] = a;
         }
     }
     __syncthreads();
+    const int cnt = s_kept;
     if (!active) continue;
     for (int i = 0; i < cnt; i++) {
         const float a = sa[i];
@@ -1118,7 +1186,7 @@ static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const
                                     const uint32_t* index_list, const int* counts, int64_t list_lo,
                                     const LineGeom* lines, const int* line_ids, const LineTile* tiles,
                                     int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
-                                    unsigned long long* bins, cudaStream_t stream) {
+                                    unsigned long long* bins, cudaStream_t stream, const TileBox* boxes) {
     // chunks over all scatterers (for the residue list: over n, the kernel
     // returns early past the list length, which is a handful)
     int64_t chunks = (n + PAIR_CHUNK - 1) / PAIR_CHUNK;
@@ -1126,7 +1194,8 @@ static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const
     if (chunks < 1) chunks = 1;
     dim3 grid((unsigned)chunks, (unsigned)num_tiles);
     project_generic_kernel<BEAM, SPLINE, REF><<<grid, PAIR_THREADS, 0, stream>>>(
-        xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b);
+        xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b,
+        REF ? nullptr : boxes);
     return cudaGetLastError();
 }
 
@@ -1134,12 +1203,12 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
                                    int degree, const uint32_t* index_list, const int* counts, int64_t list_lo,
                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles, int num_tiles,
                                    const LineBasis* basis, const SimParams& p, const BeamDev& b,
-                                   unsigned long long* bins, cudaStream_t stream) {
+                                   unsigned long long* bins, cudaStream_t stream, const TileBox* boxes) {
     (void)num_cs;
     if (n <= 0 || num_tiles <= 0) return cudaSuccess;
     const bool spline = cps != nullptr;
     const bool ref = p.mode == MODE_REFERENCE;
-#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream)
+#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream, boxes)
     if (b.type == BEAM_GAUSSIAN) {
         if (spline) return ref ? BCSIM_GEN(BEAM_GAUSSIAN, true, true) : BCSIM_GEN(BEAM_GAUSSIAN, true, false);
         return ref ? BCSIM_GEN(BEAM_GAUSSIAN, false, true) : BCSIM_GEN(BEAM_GAUSSIAN, false, false);

@@ -165,7 +165,7 @@ def test_full_size_lines_vs_oracle(oracle, which):
         assert oracle.rel_rms(iq[lo:lo + 4], ref) <= FP64_TOL, (which, lo)
 
 
-@pytest.mark.parametrize("name", ["sector_pd", "sector_nopd", "lut3d", "edge"])
+@pytest.mark.parametrize("name", ["sector_pd", "sector_nopd", "lut3d", "edge", "spline", "linear"])
 def test_culling_is_exact(name):
     """Skipping (scatterer, line-slot) pairs whose weight is provably zero
     changes no bit of the output."""
@@ -222,6 +222,8 @@ def test_spline_lines_at_random_times(oracle):
     s = job.scan
     job.scan = type(s)(s.origins[perm], s.directions[perm], s.lateral_dirs[perm], s.timestamps[perm], s.line_length)
     assert np.array_equal(run(job), iq[perm])
+    # the per-tile culling (control-point boxes) changes no bit
+    assert np.array_equal(run(job, cull="off"), iq[perm])
 
 
 def test_new_frame_same_shape_matches_fresh_simulator():
