@@ -42,6 +42,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "scatterer-line projections/s"
+# DRAM traffic of one projection launch of the default workloads (ncu, full size)
+NCU_TRAFFIC_BYTES = {"volume_3d_lut": 395.11e6 + 354.82e6}
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -273,17 +275,20 @@ def run_gpu(args):
     d2h = L * nd * 8
 
     # ---- one instrumented run (outside every timed region): the (record, line)
-    # pairs the shared-origin kernel visits and those with a non-zero weight ----
+    # pairs the shared-origin kernel visits and those with a non-zero weight, and
+    # the (scatterer, line) pairs the per-pair kernel evaluates after its tile
+    # culling ----
     shared_path = "prep_sort_ms" in stage
-    visited = nonzero = idle_steps = None
+    visited = nonzero = idle_steps = per_pair = None
+    sim.set_parameter("count_pairs", "on")
+    sim.simulate_lines_device(dev_out.data_ptr(), dev_out.numel())
+    torch.cuda.synchronize()
     if shared_path:
-        sim.set_parameter("count_pairs", "on")
-        sim.simulate_lines_device(dev_out.data_ptr(), dev_out.numel())
-        torch.cuda.synchronize()
         visited = int(sim.get_debug_data("evaluated_pairs")[0])
         nonzero = int(sim.get_debug_data("weighted_pairs")[0])
         idle_steps = int(sim.get_debug_data("idle_walk_steps")[0])
-        sim.set_parameter("count_pairs", "off")
+    per_pair = int(sim.get_debug_data("per_pair_evaluated_pairs")[0])
+    sim.set_parameter("count_pairs", "off")
 
     if rank != 0:
         return None
@@ -291,9 +296,10 @@ def run_gpu(args):
     fpp = flops_per_projection(lut, job.phase_delay, job.splines[0].degree if job.splines and not job.fixed else None)
     proj_avg_ms = statistics.mean(proj_ms)
     # units one launch processes: the pairs the shared-origin kernel visits (the
-    # others have weight exactly 0 and are skipped by the slot masks); the
-    # per-pair kernel evaluates every (scatterer, line) pair
-    units = visited if visited is not None else projections
+    # others have weight exactly 0 and are skipped by the slot masks), or the
+    # pairs the per-pair kernel evaluates (its tiles leave out scatterers none of
+    # their lines can see)
+    units = visited if shared_path else per_pair
     achieved_tflops = units * fpp / (proj_avg_ms / 1e3) / 1e12
     all_pairs_tflops = projections * fpp / (proj_avg_ms / 1e3) / 1e12
     sms = sm_count()
@@ -308,7 +314,10 @@ def run_gpu(args):
     alg_bytes = (sum(f.xyza.nbytes for f in job.fixed) +
                  sum(sp.control_points.shape[0] * (12 * sp.control_points.shape[1] + 4) for sp in job.splines) +
                  (job.beam.samples.nbytes if lut else 0) + L * nd * 8)
-    traffic = None
+    # DRAM bytes (read + write) of one projection launch, from an ncu capture of
+    # that launch at full size (dram__bytes_read.sum + dram__bytes_write.sum);
+    # --traffic-bytes overrides
+    traffic = NCU_TRAFFIC_BYTES.get(args.workload) if not (args.num_scatterers or args.lines or args.param) else None
     if args.traffic_bytes:
         traffic = float(args.traffic_bytes)
     result = {
@@ -327,12 +336,14 @@ def run_gpu(args):
                      "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tflops / fp32_peak, "traffic": traffic,
                      "flops_per_unit": fpp, "units_per_launch": units,
-                     "unit_counted": "visited (record, line) pairs" if shared_path else "(scatterer, line) pairs",
+                     "unit_counted": "visited (record, line) pairs" if shared_path
+                                     else "evaluated (scatterer, line) pairs",
                      "pairs": {"all": projections, "visited": visited, "nonzero_weight": nonzero,
+                               "per_pair_evaluated": per_pair,
                                "idle_warp_steps": idle_steps},
                      "all_pairs_convention": {"achieved": all_pairs_tflops, "frac": all_pairs_tflops / fp32_peak,
-                                              "note": "flops_per_unit x N x L: counts the pairs of weight exactly 0 "
-                                                      "that the slot masks skip, so it can exceed the peak"},
+                                              "note": "flops_per_unit x N x L: counts the pairs that the exact "
+                                                      "culling skips, so it can exceed the peak"},
                      "kernel_ms": proj_avg_ms,
                      "peak_source": f"nominal FP32 FMA rate: {sms} SMs x 128 lanes x 2 x {clock_mhz:.0f} MHz "
                                     "(median SM clock sampled during the timed steps)"},

@@ -1028,7 +1028,7 @@ void Simulator::prepare() {
     P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
     bins_.reserve(P.bins_bytes, stream_);
     counts_.reserve(4 * sizeof(int), stream_);
-    pair_counts_.reserve(3 * sizeof(unsigned long long), stream_);
+    pair_counts_.reserve(4 * sizeof(unsigned long long), stream_);
     out_.reserve((size_t)L * nd_ * sizeof(float2), stream_);
     P.spline_off.assign(splines_.size(), -1);
     if (P.n_shared > 0) {
@@ -1099,6 +1099,11 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     int launches = 0;   // kernels of this library launched (the radix sort's are counted apart)
     const LineGeom* lines_d = lines_dev_.as<LineGeom>();
     BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, st));
+    unsigned long long* pair_counts = nullptr;   // instrumented run (count_pairs)
+    if (count_pairs_ && p.mode == MODE_FP64) {
+        pair_counts = pair_counts_.as<unsigned long long>();
+        BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 4 * sizeof(unsigned long long), st));
+    }
     if (timing) debug_["kernel_memset_ms"].push_back(timer.stop());
 
     if (P.n_shared > 0) {
@@ -1132,11 +1137,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
         }
         if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
         timer.restart();
-        unsigned long long* pair_counts = nullptr;
-        if (count_pairs_ && p.mode == MODE_FP64) {
-            pair_counts = pair_counts_.as<unsigned long long>();
-            BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 3 * sizeof(unsigned long long), st));
-        }
+
         ++launches;
         BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
                                          line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins,
@@ -1148,7 +1149,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
                                                   vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
-                                                  (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
+                                                  (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
+                                                  pair_counts));
             } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
                 ++launches;
@@ -1156,7 +1158,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                                                   ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
-                                                  gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
+                                                  gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
+                                                  pair_counts));
             }
         }
         if (timing) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
@@ -1171,7 +1174,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
-                                              b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
+                                              b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
+                                                  pair_counts));
         } else {
             if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
@@ -1179,7 +1183,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
                 BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
-                                              gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr));
+                                              gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
+                                                  pair_counts));
         }
     }
     if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
@@ -1203,13 +1208,14 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     if (store_details_) debug_.clear();
     const cudaStream_t st = stream_;
     enqueue(st, dev_out, store_details_);
-    if (count_pairs_ && plan_.n_shared > 0 && mode_ == MODE_FP64) {
-        unsigned long long c[3] = {0, 0, 0};
+    if (count_pairs_ && mode_ == MODE_FP64) {
+        unsigned long long c[4] = {0, 0, 0, 0};
         BCSIM_CUDA(cudaMemcpyAsync(c, pair_counts_.get(), sizeof c, cudaMemcpyDeviceToHost, st));
         BCSIM_CUDA(cudaStreamSynchronize(st));
         debug_["evaluated_pairs"] = {(double)c[0]};
         debug_["weighted_pairs"] = {(double)c[1]};
         debug_["idle_walk_steps"] = {(double)c[2]};
+        debug_["per_pair_evaluated_pairs"] = {(double)c[3]};
     }
     if (host_out) {
         EventTimer timer(store_details_, st);

@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                            int64_t list_lo, const LineGeom* __restrict__ lines, const int* __restrict__ line_ids,
                            const LineTile* __restrict__ tiles, const LineBasis* __restrict__ basis,
                            unsigned long long* __restrict__ bins, SimParams p, BeamDev b,
-                           const TileBox* __restrict__ boxes) {
+                           const TileBox* __restrict__ boxes, unsigned long long* __restrict__ pair_counts) {
     __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? MAX_SPLINE_DEGREE + 1 : 1)];
     __shared__ float sa[PAIR_CHUNK];
     __shared__ int s_kept;   // scatterers of the chunk kept for the tile
@@ -914,6 +914,8 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     }
     __syncthreads();
     const int cnt = s_kept;
+    // instrumented run: the (scatterer, line) pairs this tile evaluates
+    if (pair_counts && tid == 0 && cnt > 0) atomicAdd(pair_counts + 3, (unsigned long long)cnt * tile.count);
     if (!active) continue;
     for (int i = 0; i < cnt; i++) {
         const float a = sa[i];
@@ -1186,7 +1188,8 @@ static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const
                                     const uint32_t* index_list, const int* counts, int64_t list_lo,
                                     const LineGeom* lines, const int* line_ids, const LineTile* tiles,
                                     int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
-                                    unsigned long long* bins, cudaStream_t stream, const TileBox* boxes) {
+                                    unsigned long long* bins, cudaStream_t stream, const TileBox* boxes,
+                                    unsigned long long* pair_counts) {
     // chunks over all scatterers (for the residue list: over n, the kernel
     // returns early past the list length, which is a handful)
     int64_t chunks = (n + PAIR_CHUNK - 1) / PAIR_CHUNK;
@@ -1195,7 +1198,7 @@ static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const
     dim3 grid((unsigned)chunks, (unsigned)num_tiles);
     project_generic_kernel<BEAM, SPLINE, REF><<<grid, PAIR_THREADS, 0, stream>>>(
         xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b,
-        REF ? nullptr : boxes);
+        REF ? nullptr : boxes, pair_counts);
     return cudaGetLastError();
 }
 
@@ -1203,12 +1206,13 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
                                    int degree, const uint32_t* index_list, const int* counts, int64_t list_lo,
                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles, int num_tiles,
                                    const LineBasis* basis, const SimParams& p, const BeamDev& b,
-                                   unsigned long long* bins, cudaStream_t stream, const TileBox* boxes) {
+                                   unsigned long long* bins, cudaStream_t stream, const TileBox* boxes,
+                                   unsigned long long* pair_counts) {
     (void)num_cs;
     if (n <= 0 || num_tiles <= 0) return cudaSuccess;
     const bool spline = cps != nullptr;
     const bool ref = p.mode == MODE_REFERENCE;
-#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream, boxes)
+#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream, boxes, pair_counts)
     if (b.type == BEAM_GAUSSIAN) {
         if (spline) return ref ? BCSIM_GEN(BEAM_GAUSSIAN, true, true) : BCSIM_GEN(BEAM_GAUSSIAN, true, false);
         return ref ? BCSIM_GEN(BEAM_GAUSSIAN, false, true) : BCSIM_GEN(BEAM_GAUSSIAN, false, false);
