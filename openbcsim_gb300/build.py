@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 
 CU_SOURCES = ["project.cu", "conv.cu", "noalloc.cu", "ingest.cu"]
 CPP_SOURCES = ["engine.cpp", "host_dsp.cpp", "capi.cpp", "batch.cpp", "server.cpp"]
-HEADERS = ["kernels.hpp", "dfloat.cuh", "fixedpoint.cuh", "engine.hpp", "host_dsp.hpp"]
+HEADERS = ["kernels.hpp", "dfloat.cuh", "fixedpoint.cuh", "async_copy.cuh", "engine.hpp", "host_dsp.hpp"]
 
 HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-Wall", "-Wno-unused-function", "-pthread"]
 

@@ -7,24 +7,37 @@
 // every sample (CpuAlgorithm.cpp:353-358) and then keeps every D-th
 // (CpuAlgorithm.cpp:362-365).  That is a circular convolution
 //     y[k] = sum_n h_a[n] * bins[(k - n) mod M],  h_a = IFFT(FFT_M(h) * mask),
-// and only k = center + m*D, m < ceil(ns/D), is ever used.  This kernel
-// evaluates exactly those outputs as a direct FIR over the window of h_a taps
+// and only k = center + m*D, m < ceil(ns/D), is ever used.  These kernels
+// evaluate exactly those outputs as a direct FIR over the window of h_a taps
 // that holds all but a stated fraction of its energy (chosen on the host), then
-// applies the demodulation factor of output m.
+// apply the demodulation factor of output m.
 //
-// Layout: one CTA per (line, block of THREADS*4 outputs).  The bins the block
-// needs are converted from fixed point and staged in shared memory split into D
-// polyphase rows: with q = (m - m0) * D + (W - 1 - w) the segment index of tap w
-// of output m, row q mod D holds the elements of one phase, so that a phase's
+// Work item: one line and a block of consecutive outputs m0 .. m0+P-1.  The
+// bins the item needs (its segment: columns of D consecutive bins) are
+// converted from fixed point and staged in shared memory split into D
+// polyphase rows: with q = (m - m0) * D + (W - 1 - w) the segment index of tap
+// w of output m, row q mod D holds the elements of one phase, so that a phase's
 // taps walk along one row.  Each thread computes 4 consecutive outputs; along a
 // row they need consecutive elements, held in a rotating window of 4 registers:
-// one shared-memory load and one (broadcast) tap load per 16 complex MACs.  A
-// row is stored as 4 sub-rows by element index mod 4 (element e at sub-row e&3,
-// position e>>2), so that the 32 threads of a warp, whose windows start 4
-// elements apart, read 32 consecutive elements of one sub-row (no bank
-// conflicts); sub-rows are padded to 4 mod 16 elements so that the staging
-// stores, which cover all four sub-rows, do not conflict either.  The taps are
-// stored phase-major on the host, zero-padded to a multiple of 4 per phase.
+// one shared-memory load and one (broadcast) tap load per 4 complex MACs per
+// output.  A row is stored as 4 sub-rows by element index mod 4 (element e at
+// sub-row e&3, position e>>2), so that the 32 threads of a warp, whose windows
+// start 4 elements apart, read 32 consecutive elements of one sub-row (no bank
+// conflicts).  The staging writes element q (column q / D, phase q % D) for
+// consecutive q from consecutive threads; sub-rows of odd length and rows of
+// length 2 mod 16 (in float2) keep those stores free of bank conflicts for
+// D = 8.  The taps are stored phase-major on the host, zero-padded to a
+// multiple of 4 per phase.
+//
+// One CTA per work item (blockIdx.y = line, blockIdx.x = output block): the
+// threads load the segment's bins with coalesced 16-byte loads (eight in
+// flight per thread), convert them and store the phase rows; while one CTA
+// convolves, the SM's other resident CTAs load theirs.
+//
+// Complex MACs use three real products (Gauss): for bin a + ib and tap c + id,
+//     k1 += c (a + b),   (k2, k3) += (a (d - c), b (c + d))   (one FFMA2),
+//     re = k1 - k3,  im = k1 + k2,
+// three FMA-pipe lane operations per complex MAC instead of four.
 #include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -35,31 +48,139 @@ namespace bcsim_gb300 {
 
 constexpr int CONV_K = 4;   // outputs per thread
 
-// Complex multiply-accumulate y += v h with paired FP32 FMAs (two per
-// instruction): the tap is held as (h.re, h.im, -h.im, h.re), so that
-//     y += (v.im, v.im) * (-h.im, h.re),   y += (v.re, v.re) * (h.re, h.im)
-// are two FFMA2 -- per component the same two fused operations, in the same
-// order, as fma(v.re, h.re, fma(-v.im, h.im, y.re)) and its imaginary twin.
-__device__ __forceinline__ void cmac(float2& y, float2 v, float4 h) {
-    y = __ffma2_rn(make_float2(v.y, v.y), make_float2(h.z, h.w), y);
-    y = __ffma2_rn(make_float2(v.x, v.x), make_float2(h.x, h.y), y);
-}
-// real bins (no phase delay): y += v.re h
+// real bins (no phase delay): y += v.re h with h = (c, d)
 __device__ __forceinline__ void rmac(float2& y, float2 v, float4 h) {
     y = __ffma2_rn(make_float2(v.x, v.x), make_float2(h.x, h.y), y);
 }
-__device__ __forceinline__ float4 tap4(float2 h) { return make_float4(h.x, h.y, -h.y, h.x); }
+// tap c + id in the form the MAC loop reads: (d - c, c + d, c, 0) for complex
+// bins (Gauss), (c, d, 0, 0) for real bins
+__device__ __forceinline__ float4 tap_gauss(float2 h) { return make_float4(h.y - h.x, h.x + h.y, h.x, 0.0f); }
+__device__ __forceinline__ float4 tap_real(float2 h) { return make_float4(h.x, h.y, 0.0f, 0.0f); }
 
+// Fixed-point bin -> float (times inv_scale = 2^-S).  The magnitude is split
+// as hi * 2^32 + lo; hi * 2^32 + float(lo) is rounded once by the FMA and
+// float(lo) once before it, so the error is at most 2^7 units of the
+// fixed-point scale plus half an FP32 ulp of the result -- 2^-54 of the scale's
+// range bound 2^61, far below the FP32 resolution of any bin that matters --
+// and conversion is odd (-v converts to exactly minus v's value).  No FP64 or
+// 64-bit multiply instruction is involved.
+__device__ __forceinline__ float fix2f(long long v, float inv_scale) {
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    const float r = fmaf(__uint2float_rn((unsigned)(a >> 32)), 4294967296.0f, __uint2float_rn((unsigned)a)) * inv_scale;
+    return v < 0 ? -r : r;
+}
+
+// Row padding (in float2) that makes a row 2 mod 16 long: consecutive phases of
+// one column then fall on different bank pairs.
+__host__ __device__ __forceinline__ int conv_rowpad(int sub) { return ((2 - 4 * sub) % 16 + 16) % 16; }
+
+// The MAC loop of one thread: outputs 4*tid .. 4*tid+3 of the staged item, over
+// all D phases.  seg: [D][row] with 4 sub-rows of `sub` positions per row;
+// tp4: taps in shared memory (TAPS_SMEM) else taps_pm in global memory;
+// ph: phase offsets into the phase-major taps (D + 1 entries).
+//
+// Iteration i of a phase covers taps 4i .. 4i+3: it needs row elements
+// r0[i], r1[i], r2[i] (from iteration i-1), r3[i], r0[i+1], r1[i+1], r2[i+1]
+// and four taps.  Three register sets rotate: iteration i computes from set
+// i mod 3 (loaded during iteration i-1) and the carried elements of set
+// (i-1) mod 3, and loads set (i+1) mod 3 for the next iteration -- every
+// shared-memory load has a whole iteration to land, with no register moves.
+struct FirSet {
+    float2 a, b, c, d;        // r3[i], r0[i+1], r1[i+1], r2[i+1]
+    float sa, sb, sc, sd;     // their re + im (complex bins)
+    float4 h0, h1, h2, h3;    // taps 4i .. 4i+3
+};
+
+template <bool PD, bool TAPS_SMEM>
+__device__ __forceinline__ void fir_mac(const float2* seg, int row, int sub, int tid, const float4* tp4,
+                                        const float2* __restrict__ taps_pm, const int* ph, int D, float2 out[4]) {
+    float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
+    float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
+    for (int p = 0; p < D; p++) {
+        // element tid*4 + t + j of the phase row: sub-row j & 3, position tid + t/4 + j/4
+        const float2* r0 = seg + p * row + tid;
+        const float2* r1 = r0 + sub;
+        const float2* r2 = r1 + sub;
+        const float2* r3 = r2 + sub;
+        const int t_beg = ph[p];
+        const int n4 = (ph[p + 1] - t_beg) >> 2;
+        if (n4 == 0) continue;
+        const float4* hp = tp4 + t_beg;
+        const float2* hg = taps_pm + t_beg;
+        auto tap = [&](int t) -> float4 {
+            return TAPS_SMEM ? hp[t] : (PD ? tap_gauss(__ldg(hg + t)) : tap_real(__ldg(hg + t)));
+        };
+        FirSet S0, S1, S2;
+#define BCSIM_LOAD(S, I)                                                            \
+    {                                                                               \
+        S.a = r3[I]; S.b = r0[(I) + 1]; S.c = r1[(I) + 1]; S.d = r2[(I) + 1];       \
+        S.h0 = tap(4 * (I)); S.h1 = tap(4 * (I) + 1); S.h2 = tap(4 * (I) + 2); S.h3 = tap(4 * (I) + 3); \
+    }
+#define BCSIM_MAC(Y, Z, W, SW, H)                                                   \
+    {                                                                               \
+        if (PD) { Y = __ffma2_rn(W, make_float2(H.x, H.y), Y); Z = fmaf(SW, H.z, Z); } \
+        else rmac(Y, W, H);                                                         \
+    }
+#define BCSIM_ITER(C, P, N, I)                                                      \
+    {                                                                               \
+        if ((I) + 1 < n4) BCSIM_LOAD(N, (I) + 1)                                    \
+        if (PD) { C.sa = C.a.x + C.a.y; C.sb = C.b.x + C.b.y; C.sc = C.c.x + C.c.y; C.sd = C.d.x + C.d.y; } \
+        BCSIM_MAC(y0, z0, P.b, P.sb, C.h0) BCSIM_MAC(y1, z1, P.c, P.sc, C.h0)       \
+        BCSIM_MAC(y2, z2, P.d, P.sd, C.h0) BCSIM_MAC(y3, z3, C.a, C.sa, C.h0)       \
+        BCSIM_MAC(y0, z0, P.c, P.sc, C.h1) BCSIM_MAC(y1, z1, P.d, P.sd, C.h1)       \
+        BCSIM_MAC(y2, z2, C.a, C.sa, C.h1) BCSIM_MAC(y3, z3, C.b, C.sb, C.h1)       \
+        BCSIM_MAC(y0, z0, P.d, P.sd, C.h2) BCSIM_MAC(y1, z1, C.a, C.sa, C.h2)       \
+        BCSIM_MAC(y2, z2, C.b, C.sb, C.h2) BCSIM_MAC(y3, z3, C.c, C.sc, C.h2)       \
+        BCSIM_MAC(y0, z0, C.a, C.sa, C.h3) BCSIM_MAC(y1, z1, C.b, C.sb, C.h3)       \
+        BCSIM_MAC(y2, z2, C.c, C.sc, C.h3) BCSIM_MAC(y3, z3, C.d, C.sd, C.h3)       \
+    }
+        // the elements carried into iteration 0: r0[0], r1[0], r2[0]
+        S2.b = r0[0]; S2.c = r1[0]; S2.d = r2[0];
+        if (PD) { S2.sb = S2.b.x + S2.b.y; S2.sc = S2.c.x + S2.c.y; S2.sd = S2.d.x + S2.d.y; }
+        BCSIM_LOAD(S0, 0)
+        for (int i = 0;; i += 3) {
+            BCSIM_ITER(S0, S2, S1, i)
+            if (i + 1 >= n4) break;
+            BCSIM_ITER(S1, S0, S2, i + 1)
+            if (i + 2 >= n4) break;
+            BCSIM_ITER(S2, S1, S0, i + 2)
+            if (i + 3 >= n4) break;
+        }
+#undef BCSIM_ITER
+#undef BCSIM_MAC
+#undef BCSIM_LOAD
+    }
+    if (PD) {   // re = k1 - k3, im = k1 + k2 with k1 = z, (k2, k3) = y
+        out[0] = make_float2(z0 - y0.y, z0 + y0.x); out[1] = make_float2(z1 - y1.y, z1 + y1.x);
+        out[2] = make_float2(z2 - y2.y, z2 + y2.x); out[3] = make_float2(z3 - y3.y, z3 + y3.x);
+    } else {
+        out[0] = y0; out[1] = y1; out[2] = y2; out[3] = y3;
+    }
+}
+
+// Demodulated outputs m0 + 4*tid + k (k < 4, m < nd) of one line.
+__device__ __forceinline__ void fir_store(const float2 ys[4], int64_t line, int m0, int tid, int nd,
+                                          const float2* __restrict__ demod, float2* __restrict__ out) {
+#pragma unroll
+    for (int k = 0; k < CONV_K; k++) {
+        const int m = m0 + tid * CONV_K + k;
+        if (m < nd) {
+            const float2 dm = __ldg(demod + m);
+            out[line * nd + m] = make_float2(ys[k].x * dm.x - ys[k].y * dm.y, ys[k].x * dm.y + ys[k].y * dm.x);
+        }
+    }
+}
+
+// One work item per CTA: line blockIdx.y, outputs blockIdx.x * blockDim.x * 4 ...
 template <bool PD, bool TAPS_SMEM>
 __global__ void __launch_bounds__(128)
     convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
                                const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
-                               int tap_start, int64_t M, int center, int D, int nd, int sub, int cols,
+                               int tap_start, int64_t M, int center, int D, int nd, int sub, int row, int cols,
                                const float2* __restrict__ demod, float2* __restrict__ out) {
-    extern __shared__ float4 smem4[];
-    float2* seg = reinterpret_cast<float2*>(smem4);   // [D][4][sub]
-    const int row = 4 * sub;
-    // phase-major taps as (h.re, h.im, -h.im, h.re), in shared memory when they fit
+    extern __shared__ __align__(16) float4 smem4[];
+    float2* seg = reinterpret_cast<float2*>(smem4);   // [D][row]
+    // phase-major taps, in shared memory when they fit
     float4* tp4 = reinterpret_cast<float4*>(seg + (size_t)D * row);
     const int line = blockIdx.y;
     const int per_cta = blockDim.x * CONV_K;
@@ -67,12 +188,10 @@ __global__ void __launch_bounds__(128)
     const int tid = threadIdx.x;
     if (TAPS_SMEM) {
         const int ntaps_pm = __ldg(ph_off + D);
-        for (int i = tid; i < ntaps_pm; i += blockDim.x) tp4[i] = tap4(__ldg(taps_pm + i));
+        for (int i = tid; i < ntaps_pm; i += blockDim.x)
+            tp4[i] = PD ? tap_gauss(__ldg(taps_pm + i)) : tap_real(__ldg(taps_pm + i));
     }
-    // bins index of segment element q = col * D + ph: j = (jbase + q) mod M, M a
-    // power of two (next_power_of_two, fft.cpp:80-82), so the wrap is a mask
-    const int64_t k0 = (int64_t)center + (int64_t)m0 * D;
-    const int64_t jbase = k0 - tap_start - (W - 1);
+    const long long jbase = (long long)center + (long long)m0 * D - tap_start - (W - 1);
     const long long mmask = (long long)M - 1;
     const int stride = PD ? 2 : 1;
     const long long* lb = (const long long*)bins + (int64_t)line * ns * stride;
@@ -80,75 +199,56 @@ __global__ void __launch_bounds__(128)
     // the columns its threads read
     const int valid = min(per_cta, nd - m0);
     const int cols_used = min(cols, ((valid + CONV_K - 1) / CONV_K) * CONV_K + (cols - CONV_K * (int)blockDim.x));
-    // each thread stages the D consecutive bins of a column (one or two cache
-    // lines, read once), writing one element of every phase row
-    for (int col = tid; col < cols_used; col += blockDim.x) {
-        const long long j0 = jbase + (long long)col * D;
-        float2* dst = seg + (col & 3) * sub + (col >> 2);
-        for (int ph = 0; ph < D; ph++) {
-            const long long j = (j0 + ph) & mmask;
-            float2 v = make_float2(0.0f, 0.0f);
-            if (j < ns) {
-                if (PD) {
-                    const longlong2 q = __ldg(reinterpret_cast<const longlong2*>(lb) + j);
-                    v.x = ll2f_rn(q.x) * inv_scale;
-                    v.y = ll2f_rn(q.y) * inv_scale;
-                } else {
-                    v.x = ll2f_rn(__ldg(lb + j)) * inv_scale;
-                }
+    // element q of the segment (column q / D, phase q % D) is bin jbase + q:
+    // consecutive threads read consecutive bins, 8 loads in flight per thread
+    const int nelem = cols_used * D;
+    const int step_c = blockDim.x / D, step_p = blockDim.x - step_c * D;
+    const int big_c = (8 * blockDim.x) / D, big_p = 8 * blockDim.x - big_c * D;
+    int col_t = tid / D, ph_t = tid - col_t * D;   // (column, phase) of element q0
+    for (int q0 = tid; q0 < nelem; q0 += 8 * blockDim.x) {
+        longlong2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int q = q0 + u * (int)blockDim.x;
+            const long long j = (jbase + q) & mmask;
+            v[u] = make_longlong2(0, 0);
+            if (q < nelem && j < ns) {
+                if (PD) v[u] = __ldg(reinterpret_cast<const longlong2*>(lb) + j);
+                else v[u].x = __ldg(lb + j);
             }
-            dst[ph * row] = v;
         }
+        int c = col_t, p = ph_t;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (q0 + u * (int)blockDim.x < nelem)
+                seg[p * row + (c & 3) * sub + (c >> 2)] =
+                    make_float2(fix2f(v[u].x, inv_scale), PD ? fix2f(v[u].y, inv_scale) : 0.0f);
+            c += step_c;
+            p += step_p;
+            if (p >= D) { p -= D; c++; }
+        }
+        col_t += big_c;
+        ph_t += big_p;
+        if (ph_t >= D) { ph_t -= D; col_t++; }
     }
     __syncthreads();
     if (tid * CONV_K >= valid) return;   // no output of this thread (no barrier follows)
-    float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
-    for (int ph = 0; ph < D; ph++) {
-        // element tid*4 + t + j of the phase row: sub-row j & 3, position tid + t/4 + j/4
-        const float2* r0 = seg + ph * row + tid;
-        const float2* r1 = r0 + sub;
-        const float2* r2 = r1 + sub;
-        const float2* r3 = r2 + sub;
-        const int t_beg = __ldg(ph_off + ph), t_end = __ldg(ph_off + ph + 1);
-        float2 w0 = r0[0], w1 = r1[0], w2 = r2[0], w3;
-        const float4* hp = tp4 + t_beg;
-        const float2* hg = taps_pm + t_beg;
-        for (int t = 0, i = 0; t < t_end - t_beg; t += 4, i++) {
-            float4 h;
-            w3 = r3[i]; h = TAPS_SMEM ? hp[t] : tap4(__ldg(hg + t));
-            if (PD) { cmac(y0, w0, h); cmac(y1, w1, h); cmac(y2, w2, h); cmac(y3, w3, h); }
-            else { rmac(y0, w0, h); rmac(y1, w1, h); rmac(y2, w2, h); rmac(y3, w3, h); }
-            w0 = r0[i + 1]; h = TAPS_SMEM ? hp[t + 1] : tap4(__ldg(hg + t + 1));
-            if (PD) { cmac(y0, w1, h); cmac(y1, w2, h); cmac(y2, w3, h); cmac(y3, w0, h); }
-            else { rmac(y0, w1, h); rmac(y1, w2, h); rmac(y2, w3, h); rmac(y3, w0, h); }
-            w1 = r1[i + 1]; h = TAPS_SMEM ? hp[t + 2] : tap4(__ldg(hg + t + 2));
-            if (PD) { cmac(y0, w2, h); cmac(y1, w3, h); cmac(y2, w0, h); cmac(y3, w1, h); }
-            else { rmac(y0, w2, h); rmac(y1, w3, h); rmac(y2, w0, h); rmac(y3, w1, h); }
-            w2 = r2[i + 1]; h = TAPS_SMEM ? hp[t + 3] : tap4(__ldg(hg + t + 3));
-            if (PD) { cmac(y0, w3, h); cmac(y1, w0, h); cmac(y2, w1, h); cmac(y3, w2, h); }
-            else { rmac(y0, w3, h); rmac(y1, w0, h); rmac(y2, w1, h); rmac(y3, w2, h); }
-        }
-    }
-    const float2 ys[CONV_K] = {y0, y1, y2, y3};
-    const int base = tid * CONV_K;
-#pragma unroll
-    for (int k = 0; k < CONV_K; k++) {
-        const int m = m0 + base + k;
-        if (m < nd) {
-            const float2 dm = __ldg(demod + m);
-            out[(int64_t)line * nd + m] = make_float2(ys[k].x * dm.x - ys[k].y * dm.y, ys[k].x * dm.y + ys[k].y * dm.x);
-        }
-    }
+    float2 ys[CONV_K];
+    fir_mac<PD, TAPS_SMEM>(seg, row, sub, tid, tp4, taps_pm, ph_off, D, ys);
+    fir_store(ys, line, m0, tid, nd, demod, out);
 }
 
-// Staged elements per phase row for a block of `threads` threads: thread T's
-// window reaches element 4T + max_ph_taps + 2, so 4*threads + max_ph_taps
-// elements (max_ph_taps is a multiple of 4) cover every read.
-static int conv_cols(int threads, int max_ph_taps) { return threads * CONV_K + max_ph_taps; }
-// Sub-row length: cols/4 positions, padded to 4 mod 16.
-static int conv_sub(int threads, int max_ph_taps) {
-    const int need = conv_cols(threads, max_ph_taps) / 4;
-    return need + ((4 - need) % 16 + 16) % 16;
+// Staged elements per phase row for `outputs` outputs: thread T's window reaches
+// element 4T + max_ph_taps + 2, so 4*ceil(outputs/4) + max_ph_taps elements
+// (max_ph_taps is a multiple of 4) cover every read.
+static int conv_cols(int outputs, int max_ph_taps) {
+    return (outputs + CONV_K - 1) / CONV_K * CONV_K + max_ph_taps;
+}
+// Sub-row length: cols/4 positions, odd.
+static int conv_sub(int cols) { return (cols / 4) | 1; }
+static int conv_row(int cols) {
+    const int sub = conv_sub(cols);
+    return 4 * sub + conv_rowpad(sub);
 }
 
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
@@ -157,35 +257,45 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
                                        int nd, const float2* demod, float2* out, cudaStream_t stream) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
     if (max_ph_taps % 4) return cudaErrorInvalidValue;
-    // a line's outputs split evenly over its blocks of at most 128 threads
-    // (4 outputs each; no block left nearly empty), and more blocks per line
-    // for few lines so that the grid still fills the GPU
+    const int D = decimation;
+    int dev = 0, sms = 0, smem_optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    const size_t limit = std::min<size_t>(200 * 1024, (size_t)smem_optin);
+
+    // a line's outputs split evenly over blocks of at most 128 threads (4
+    // outputs each; no block left nearly empty), more blocks per line only
+    // while the grid has fewer CTAs than SMs (more, smaller blocks per line
+    // measured slower: more halo per output, and a second partial wave where
+    // the first would have held the grid)
     auto threads_for = [&](int64_t blocks) {
         const int64_t per = (nd + blocks - 1) / blocks;
         return (int)std::max<int64_t>(32, ((per + CONV_K - 1) / CONV_K + 31) / 32 * 32);
     };
+
     int64_t nblk = (nd + 128 * CONV_K - 1) / (128 * CONV_K);
     int threads = threads_for(nblk);
-    while (threads > 32 && (int64_t)num_lines * nblk < 2 * 152) threads = threads_for(++nblk);
-    nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
+    while (threads > 32 && (int64_t)num_lines * nblk < sms) threads = threads_for(++nblk);
     auto smem_for = [&](int th, int taps_smem) {
-        return (size_t)4 * conv_sub(th, max_ph_taps) * decimation * sizeof(float2) +
+        return (size_t)D * conv_row(conv_cols(th * CONV_K, max_ph_taps)) * sizeof(float2) +
                (taps_smem ? (size_t)ntaps_pm * sizeof(float4) : 0);
     };
     int taps_in_smem = 1;
-    const size_t limit = 200 * 1024;
     if (smem_for(threads, 1) > limit) taps_in_smem = 0;   // very long windows: taps from global memory (broadcast loads)
     while (smem_for(threads, taps_in_smem) > limit && threads > 32) threads -= 32;
     const size_t smem = smem_for(threads, taps_in_smem);
     if (smem > limit) return cudaErrorInvalidValue;
-    const int sub = conv_sub(threads, max_ph_taps), cols = conv_cols(threads, max_ph_taps);
+    const int cols = conv_cols(threads * CONV_K, max_ph_taps);
+    const int sub = conv_sub(cols), row = conv_row(cols);
     nblk = (nd + threads * CONV_K - 1) / (threads * CONV_K);
     const dim3 grid((unsigned)nblk, (unsigned)num_lines);
     auto launch = [&](auto k) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, decimation,
-                                           nd, sub, cols, demod, out);
+        cudaError_t e2 = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e2 != cudaSuccess) return e2;
+        k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, D, nd, sub,
+                                           row, cols, demod, out);
         return cudaGetLastError();
     };
     if (phase_delay) return taps_in_smem ? launch(convolve_demodulate_kernel<true, true>)

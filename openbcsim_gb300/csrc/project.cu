@@ -31,6 +31,7 @@
 #include "kernels.hpp"
 #include "dfloat.cuh"
 #include "fixedpoint.cuh"
+#include "async_copy.cuh"
 
 namespace bcsim_gb300 {
 
@@ -352,42 +353,6 @@ __global__ void gather_records_kernel(const uint32_t* __restrict__ svals, const 
 // ---------------------------------------------------------------------------
 // shared-origin projection
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
-}
-
-// Wait for phase `parity` of the barrier, giving up after `limit` polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned limit) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
-    for (unsigned it = 0; it < limit; it++) {
-        unsigned done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
-}
-
-// 1-D TMA bulk copy global -> shared, completion counted on `bar`.
-__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, unsigned bytes, uint64_t* bar) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    const unsigned b = (unsigned)__cvta_generic_to_shared(bar);
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
-                 "l"(gsrc), "r"(bytes), "r"(b)
-                 : "memory");
-}
-
 __device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
 
 // Records per folding of the FP32 run sum into the integer bin total: bounds
