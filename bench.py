@@ -604,6 +604,65 @@ def run_serve(args):
             "server_stats": st, "per_phantom": per_phantom, "slowest_requests": slow}
 
 
+def run_imaging(args):
+    """Post-processing rows: B-mode (envelope, log compression, scan conversion)
+    of config 1's frame (128 lines x 780 samples) into the image size the
+    reference's GUI uses (70 degree sector, 12 cm, 6000 dots per metre), and the
+    colour-Doppler estimate + image of a 16-frame packet of it.  GPU: frames/s
+    through the C ABI with host IQ in and the image out (host clock), and
+    simulate_bmode (simulation + image, the IQ staying on the device).  CPU: the
+    oracle's restatement of the same steps, one host thread."""
+    import openbcsim_gb300 as gb
+    from oracle import imaging as OI
+    from openbcsim_gb300 import workloads as W
+
+    job = W.sector_2d_fixed()
+    sim = gb.RfSimulator("gpu")
+    gb.configure_job(sim, job)
+    width = float(np.float32(np.deg2rad(70.0)))
+    nx, ny = gb.ScanGeometry.image_size("sector", width, job.scan.line_length, 6000.0)
+    geo = gb.ScanGeometry("sector", width, job.scan.line_length, nx, ny)
+    iq = sim.simulate_lines_line_major().copy()
+    P = 16
+    rng = np.random.default_rng(5)
+    packet = (iq[None] * np.exp(1j * rng.uniform(-0.3, 0.3, (P, 1, 1)) * np.arange(P)[:, None, None])).astype(
+        np.complex64)
+
+    def timed(fn, steps):
+        for _ in range(args.warmup):
+            fn()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fn()
+        return (time.perf_counter() - t0) / steps
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    t_bmode = timed(lambda: sim.bmode_image(iq, 60.0, 1.0, 0.0, geo), args.steps * 10)
+    t_sim_bmode = timed(lambda: sim.simulate_bmode(60.0, 1.0, 0.0, geo), args.steps)
+    t_sim = timed(lambda: sim.simulate_lines_line_major(), args.steps)
+    t_doppler = timed(lambda: sim.color_doppler(packet, geo), args.steps * 10)
+    clk = clocks.stop()
+    t_cpu_bmode = timed(lambda: OI.bmode(iq, 60.0, 1.0, 0.0, geo), 3)
+    t_cpu_doppler = timed(lambda: OI.color_image(*OI.color_doppler(packet), geo), 3)
+    return {"metric": "B-mode frames/s (post-processing of an IQ frame)", "value": 1.0 / t_bmode, "unit": "frames/s",
+            "n_gpus": 1, "steps": args.steps * 10, "warmup": args.warmup, "ms_per_step": t_bmode * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"sector_2d_fixed IQ {iq.shape[0]} lines x {iq.shape[1]} samples -> "
+                                   f"{nx} x {ny} sector image (70 deg, {job.scan.line_length} m, 6000 dots/m); "
+                                   f"colour Doppler packet of {P} frames",
+                       "io": "host IQ in, image out, per step"},
+            "simulate_bmode": {"value": 1.0 / t_sim_bmode, "unit": "frames/s", "ms_per_step": t_sim_bmode * 1e3,
+                               "simulate_lines_ms": t_sim * 1e3},
+            "color_doppler": {"value": 1.0 / t_doppler, "unit": "packets/s", "ms_per_step": t_doppler * 1e3,
+                              "packet_bytes": int(packet.nbytes)},
+            "cpu_baseline": {"value": 1.0 / t_cpu_bmode, "unit": "frames/s", "cores": 1, "kind": "port",
+                             "sample": "the same frame, oracle/imaging_oracle.c (envelope, log compression, "
+                                       "Cartesianator restatement)",
+                             "color_doppler": {"value": 1.0 / t_cpu_doppler, "unit": "packets/s"}},
+            "clocks": clk}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -617,8 +676,9 @@ def main():
     ap.add_argument("--num-scatterers", type=int, default=0, help="override the workload's scatterer count")
     ap.add_argument("--lines", default="", help="override the line count (volume: 'n_az,n_el')")
     ap.add_argument("--param", action="append", default=[], help="engine parameter key=value (repeatable)")
-    ap.add_argument("--mode", default="single", choices=["single", "batch", "serve"],
-                    help="single: the headline workload; batch: 64 uneven jobs; serve: Poisson request stream")
+    ap.add_argument("--mode", default="single", choices=["single", "batch", "serve", "imaging"],
+                    help="single: the headline workload; batch: 64 uneven jobs; serve: Poisson request stream; "
+                         "imaging: B-mode and colour-Doppler post-processing")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of N and L in batch/serve modes")
     ap.add_argument("--rate", type=float, default=200.0)
@@ -637,6 +697,8 @@ def main():
         res = run_batch(args)
     elif args.mode == "serve":
         res = run_serve(args)
+    elif args.mode == "imaging":
+        res = run_imaging(args)
     else:
         res = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if res is not None:

@@ -225,6 +225,66 @@ int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const float* ori
                                  float amplitude_sum_bound, void* d_out, int64_t cap_complex, void* stream,
                                  char* err, int err_cap);
 
+/* ---- Post-processing on the device: B-mode and colour Doppler ------------
+ *
+ * The reference forms images on the host after simulate_lines, in its GUI's
+ * refresh worker (src/qt5gui/RefreshWorker.hpp:179-395) with
+ * bcsim::get_max_value / log_compress_frame (src/utils/BCSimConvenience.cpp:57-83)
+ * and CpuCartesianator (src/utils/cartesianator/Cartesianator.cpp:107-205).
+ * These entry points run the same steps as kernels on the handle's stream.
+ * Layouts: IQ complex64 [num_lines][num_samples] (a packet: [frames][lines]
+ * [samples]); beam space [beam][range]; images [ny][nx], x fastest; colour
+ * pixels 4 bytes (blue, green, red, alpha). */
+#define BCSIM_GEOMETRY_SECTOR 0
+#define BCSIM_GEOMETRY_LINEAR 1
+
+/* bcsim::SectorScanGeometry / LinearScanGeometry (src/utils/ScanGeometry.hpp:44-78)
+ * plus the Cartesianator's output size. */
+typedef struct {
+    int kind;     /* BCSIM_GEOMETRY_SECTOR or BCSIM_GEOMETRY_LINEAR      */
+    float width;  /* sector: opening angle [rad]; linear: width [m]     */
+    float depth;  /* sector: depth [m]; linear: maximum range [m]       */
+    float tilt;   /* sector: tilt [rad]; linear: unused                 */
+    int nx, ny;   /* output image size [pixels], each >= 2              */
+} bcsim_scan_geometry;
+
+/* B-mode of one IQ frame (host iq): envelope |iq|; normalisation by
+ * `normalize` (<= 0: the frame's largest envelope, as the worker's
+ * auto-normalisation); 20 log10(gain * env / normalize) mapped by dyn_range
+ * [dB] to [0, 255], clamped, truncated to bytes; scan conversion by
+ * `geometry` into image [ny][nx] (geometry and image may be NULL: beam space
+ * only).  beamspace ([num_lines][num_samples] bytes) and normalize_used may
+ * be NULL. */
+int bcsim_bmode_image(bcsim_handle* h, const float* iq, int64_t num_lines, int64_t num_samples, float dyn_range,
+                      float gain, float normalize, const bcsim_scan_geometry* geometry, uint8_t* image,
+                      uint8_t* beamspace, float* normalize_used);
+/* The same from a configured simulator: simulate_lines, then the B-mode, the
+ * IQ staying on the device. */
+int bcsim_simulate_bmode(bcsim_handle* h, float dyn_range, float gain, float normalize,
+                         const bcsim_scan_geometry* geometry, uint8_t* image, uint8_t* beamspace,
+                         float* normalize_used);
+/* Scan conversion of a float beam space [num_beams][num_range] into image [ny][nx]. */
+int bcsim_scan_convert(bcsim_handle* h, const float* beamspace, int64_t num_beams, int64_t num_range,
+                       const bcsim_scan_geometry* geometry, float* image);
+/* A colour-Doppler packet (src/qt5gui/MainWindow.cpp:664-694): packet_size
+ * frames of the configured scan, frame k with every timestamp advanced by
+ * k * prt; out complex64 [packet_size][num_lines][num_samples].  The scan
+ * sequence is left as configured. */
+int bcsim_simulate_packet(bcsim_handle* h, int packet_size, float prt, float* out, int64_t cap_complex);
+/* Autocorrelation estimates of a packet (host iq_packet, packet_size >= 2):
+ * per sample R0 = sum |x_k - mean|^2 and velocity = arg sum conj(x_k) x_(k+1)
+ * (RefreshWorker.hpp:262-300) into r0 / velocity ([num_lines][num_samples],
+ * either may be NULL); with a geometry, the colour image (power threshold
+ * 0.001 of the largest R0; red for velocity >= 0, blue below) into bgra
+ * [ny][nx][4]. */
+int bcsim_color_doppler(bcsim_handle* h, const float* iq_packet, int packet_size, int64_t num_lines,
+                        int64_t num_samples, float* r0, float* velocity, const bcsim_scan_geometry* geometry,
+                        uint8_t* bgra);
+/* The same from a configured simulator: the packet is simulated and estimated
+ * on the device. */
+int bcsim_simulate_color_doppler(bcsim_handle* h, int packet_size, float prt, float* r0, float* velocity,
+                                 const bcsim_scan_geometry* geometry, uint8_t* bgra);
+
 #ifdef __cplusplus
 }
 #endif

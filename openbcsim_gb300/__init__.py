@@ -191,6 +191,86 @@ class RfSimulator:
         self._check(self._lib.bcsim_get_total_num_scatterers(self._h, C.byref(n)))
         return n.value
 
+    # --- post-processing on the device (RefreshWorker.hpp:179-395) ---
+    def bmode_image(self, iq, dyn_range: float = 60.0, gain: float = 1.0, normalize: float = 0.0,
+                    geometry: Optional["ScanGeometry"] = None, beamspace: bool = False):
+        """B-mode of an IQ frame iq [num_lines, num_samples] complex64: log-compressed
+        beam-space bytes and, with a geometry, the scan-converted image [ny, nx]
+        uint8.  normalize <= 0 normalises by the frame's largest envelope.
+        Returns (image or None, beamspace or None, normalize_used)."""
+        iq = np.ascontiguousarray(iq, np.complex64)
+        if iq.ndim != 2:
+            raise ValueError("iq must be [num_lines, num_samples]")
+        return self._bmode(iq, dyn_range, gain, normalize, geometry, beamspace)
+
+    def simulate_bmode(self, dyn_range: float = 60.0, gain: float = 1.0, normalize: float = 0.0,
+                       geometry: Optional["ScanGeometry"] = None, beamspace: bool = False):
+        """simulate_lines followed by bmode_image, the IQ staying on the device."""
+        return self._bmode(None, dyn_range, gain, normalize, geometry, beamspace)
+
+    def _bmode(self, iq, dyn_range, gain, normalize, geometry, beamspace):
+        L, nd = (iq.shape if iq is not None else self.output_shape())
+        g = geometry.c_struct() if geometry is not None else None
+        image = np.empty((geometry.ny, geometry.nx), np.uint8) if geometry is not None else None
+        bs = np.empty((L, nd), np.uint8) if beamspace else None
+        used = C.c_float()
+        gp = C.byref(g) if g is not None else None
+        ip = image.ctypes.data_as(C.c_void_p) if image is not None else None
+        bp = bs.ctypes.data_as(C.c_void_p) if bs is not None else None
+        if iq is not None:
+            self._check(self._lib.bcsim_bmode_image(self._h, iq.ctypes.data_as(C.POINTER(C.c_float)), L, nd,
+                                                    dyn_range, gain, normalize, gp, ip, bp, C.byref(used)))
+        else:
+            self._check(self._lib.bcsim_simulate_bmode(self._h, dyn_range, gain, normalize, gp, ip, bp,
+                                                       C.byref(used)))
+        return image, bs, used.value
+
+    def scan_convert(self, beamspace, geometry: "ScanGeometry") -> np.ndarray:
+        """Scan conversion of a float beam space [num_beams, num_range] into [ny, nx] float32."""
+        b = np.ascontiguousarray(beamspace, np.float32)
+        out = np.empty((geometry.ny, geometry.nx), np.float32)
+        g = geometry.c_struct()
+        self._check(self._lib.bcsim_scan_convert(self._h, _ptr(b), b.shape[0], b.shape[1], C.byref(g), _ptr(out)))
+        return out
+
+    def simulate_packet(self, packet_size: int, prt: float) -> np.ndarray:
+        """A colour-Doppler packet: [packet_size, num_lines, num_samples] complex64, frame k
+        with every timestamp advanced by k * prt."""
+        L, nd = self.output_shape()
+        out = np.empty((packet_size, L, nd), np.complex64)
+        self._check(self._lib.bcsim_simulate_packet(self._h, packet_size, prt,
+                                                    out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        return out
+
+    def color_doppler(self, iq_packet, geometry: Optional["ScanGeometry"] = None):
+        """R0 and velocity (arg R1) [num_lines, num_samples] float32 of a packet
+        [P, num_lines, num_samples], and with a geometry the colour image [ny, nx, 4]
+        (blue, green, red, alpha).  Returns (r0, velocity, image or None)."""
+        p = np.ascontiguousarray(iq_packet, np.complex64)
+        if p.ndim != 3:
+            raise ValueError("iq_packet must be [packet_size, num_lines, num_samples]")
+        return self._doppler(p, 0, 0.0, geometry)
+
+    def simulate_color_doppler(self, packet_size: int, prt: float, geometry: Optional["ScanGeometry"] = None):
+        """simulate_packet followed by color_doppler, on the device."""
+        return self._doppler(None, packet_size, prt, geometry)
+
+    def _doppler(self, packet, packet_size, prt, geometry):
+        L, nd = (packet.shape[1:] if packet is not None else self.output_shape())
+        r0 = np.empty((L, nd), np.float32)
+        vel = np.empty((L, nd), np.float32)
+        g = geometry.c_struct() if geometry is not None else None
+        img = np.empty((geometry.ny, geometry.nx, 4), np.uint8) if geometry is not None else None
+        gp = C.byref(g) if g is not None else None
+        ip = img.ctypes.data_as(C.c_void_p) if img is not None else None
+        if packet is not None:
+            self._check(self._lib.bcsim_color_doppler(self._h, packet.ctypes.data_as(C.POINTER(C.c_float)),
+                                                      packet.shape[0], L, nd, _ptr(r0), _ptr(vel), gp, ip))
+        else:
+            self._check(self._lib.bcsim_simulate_color_doppler(self._h, packet_size, prt, _ptr(r0), _ptr(vel), gp,
+                                                               ip))
+        return r0, vel, img
+
     def set_logger(self, fn):
         """fn(level: int, message: str) receives the engine's log messages; None silences."""
         if fn is None:
@@ -199,6 +279,27 @@ class RfSimulator:
             return
         self._log_cb = _capi.LOG_FN(lambda lvl, msg, user: fn(int(lvl), msg.decode()))
         self._check(self._lib.bcsim_set_logger(self._h, self._log_cb, None))
+
+
+class ScanGeometry:
+    """A sector or linear scan geometry with the output image size
+    (bcsim::SectorScanGeometry / LinearScanGeometry, src/utils/ScanGeometry.hpp:44-78)."""
+
+    def __init__(self, kind: str, width: float, depth: float, nx: int, ny: int, tilt: float = 0.0):
+        if kind not in ("sector", "linear"):
+            raise ValueError("kind must be 'sector' or 'linear'")
+        self.kind, self.width, self.depth, self.tilt, self.nx, self.ny = kind, width, depth, tilt, int(nx), int(ny)
+
+    @staticmethod
+    def image_size(kind: str, width: float, depth: float, dots_per_meter: float, tilt: float = 0.0):
+        """(nx, ny) the reference's worker uses: the Cartesian extent in metres times
+        dots per metre, truncated (RefreshWorker.hpp:192-199, ScanGeometry.hpp:49-55)."""
+        from . import _imaging_host as H
+        return H.image_size(kind, width, depth, dots_per_meter, tilt)
+
+    def c_struct(self):
+        return _capi.ScanGeometryC(_capi.GEOMETRY_SECTOR if self.kind == "sector" else _capi.GEOMETRY_LINEAR,
+                                   self.width, self.depth, self.tilt, self.nx, self.ny)
 
 
 def configure_job(sim: RfSimulator, job, precision_mode: str = "fp64"):

@@ -58,11 +58,31 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), C.c_int]),
     ("bcsim_server_stats", C.c_int, [C.c_void_p, _i64p, _i64p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      _i64p, _i64p, _i64p]),
+    ("bcsim_bmode_image", C.c_int, [C.c_void_p, _f32p, C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, _f32p]),
+    ("bcsim_simulate_bmode", C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, _f32p]),
+    ("bcsim_scan_convert", C.c_int, [C.c_void_p, _f32p, C.c_int64, C.c_int64, C.c_void_p, _f32p]),
+    ("bcsim_simulate_packet", C.c_int, [C.c_void_p, C.c_int, C.c_float, _f32p, C.c_int64]),
+    ("bcsim_color_doppler", C.c_int, [C.c_void_p, _f32p, C.c_int, C.c_int64, C.c_int64, _f32p, _f32p, C.c_void_p,
+                                      C.c_void_p]),
+    ("bcsim_simulate_color_doppler", C.c_int, [C.c_void_p, C.c_int, C.c_float, _f32p, _f32p, C.c_void_p,
+                                               C.c_void_p]),
     ("bcsim_simulate_fixed_noalloc", C.c_int,
      [C.c_void_p, C.c_int64, _f32p, _f32p, _f32p, C.c_int, C.c_float, C.c_float, _f32p, C.c_int, C.c_int,
       C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, C.c_int64,
       C.c_void_p, C.c_char_p, C.c_int]),
 ]
+
+
+
+class ScanGeometryC(C.Structure):
+    """bcsim_scan_geometry"""
+    _fields_ = [("kind", C.c_int), ("width", C.c_float), ("depth", C.c_float), ("tilt", C.c_float),
+                ("nx", C.c_int), ("ny", C.c_int)]
+
+
+GEOMETRY_SECTOR, GEOMETRY_LINEAR = 0, 1
 
 _lib = None
 

@@ -9,12 +9,15 @@
 
 #include "../../include/bcsim_gb300.h"
 #include "engine.hpp"
+#include "imaging_host.hpp"
 
 // Message of the last bcsim_create failure on this thread (no handle exists to hold it).
 static thread_local std::string g_create_error;
 
 struct bcsim_handle {
     bcsim_gb300::Simulator sim;
+    bcsim_gb300::ImagingBuffers imaging;
+    bcsim_gb300::DeviceBuffer packet;   // device IQ of the imaging entry points
     std::string last_error;
 };
 
@@ -183,6 +186,117 @@ int bcsim_get_debug_data(const bcsim_handle* hc, const char* key, double* out, i
         if ((int64_t)v.size() > cap || (!out && !v.empty()))
             throw bcsim_gb300::SimError(BCSIM_E_CAPACITY, "buffer too small");
         for (size_t i = 0; i < v.size(); i++) out[i] = v[i];
+    });
+}
+
+namespace {
+bcsim_gb300::ScanGeometry2D to_geometry(const bcsim_scan_geometry* g) {
+    return bcsim_gb300::ScanGeometry2D{g->kind, g->width, g->depth, g->tilt, g->nx, g->ny};
+}
+}  // namespace
+
+int bcsim_bmode_image(bcsim_handle* h, const float* iq, int64_t num_lines, int64_t num_samples, float dyn_range,
+                      float gain, float normalize, const bcsim_scan_geometry* geometry, uint8_t* image,
+                      uint8_t* beamspace, float* normalize_used) {
+    return guarded(h, [&] {
+        using bcsim_gb300::SimError;
+        if (!iq || num_lines <= 0 || num_samples <= 0) throw SimError(BCSIM_E_INVALID, "No lines returned");
+        if (geometry && !image) throw SimError(BCSIM_E_INVALID, "null image pointer");
+        const cudaStream_t st = h->sim.stream();
+        const size_t bytes = (size_t)num_lines * num_samples * sizeof(float2);
+        h->packet.reserve(bytes, st);
+        if (cudaMemcpyAsync(h->packet.get(), iq, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            throw SimError(BCSIM_E_CUDA, "IQ upload failed");
+        bcsim_gb300::ScanGeometry2D g{};
+        if (geometry) g = to_geometry(geometry);
+        bcsim_gb300::bmode_from_device(st, h->imaging, h->packet.as<float2>(), num_lines, num_samples, dyn_range, gain,
+                                       normalize, geometry ? &g : nullptr, image, beamspace, normalize_used);
+    });
+}
+
+int bcsim_simulate_bmode(bcsim_handle* h, float dyn_range, float gain, float normalize,
+                         const bcsim_scan_geometry* geometry, uint8_t* image, uint8_t* beamspace,
+                         float* normalize_used) {
+    return guarded(h, [&] {
+        using bcsim_gb300::SimError;
+        if (geometry && !image) throw SimError(BCSIM_E_INVALID, "null image pointer");
+        int64_t L = 0, nd = 0;
+        h->sim.output_shape(&L, &nd);
+        const cudaStream_t st = h->sim.stream();
+        h->packet.reserve((size_t)L * nd * sizeof(float2), st);
+        h->sim.simulate_device(h->packet.get(), L * nd);
+        bcsim_gb300::ScanGeometry2D g{};
+        if (geometry) g = to_geometry(geometry);
+        bcsim_gb300::bmode_from_device(st, h->imaging, h->packet.as<float2>(), L, nd, dyn_range, gain, normalize,
+                                       geometry ? &g : nullptr, image, beamspace, normalize_used);
+        h->sim.check_device_flag();
+    });
+}
+
+int bcsim_scan_convert(bcsim_handle* h, const float* beamspace, int64_t num_beams, int64_t num_range,
+                       const bcsim_scan_geometry* geometry, float* image) {
+    return guarded(h, [&] {
+        if (!beamspace || !geometry || !image) throw bcsim_gb300::SimError(BCSIM_E_INVALID, "null pointer");
+        bcsim_gb300::scan_convert_host(h->sim.stream(), h->imaging, beamspace, num_beams, num_range,
+                                       to_geometry(geometry), image);
+    });
+}
+
+int bcsim_simulate_packet(bcsim_handle* h, int packet_size, float prt, float* out, int64_t cap_complex) {
+    return guarded(h, [&] {
+        using bcsim_gb300::SimError;
+        int64_t L = 0, nd = 0;
+        h->sim.output_shape(&L, &nd);
+        if (packet_size < 1) throw SimError(BCSIM_E_INVALID, "packet size must be at least 1");
+        const int64_t total = (int64_t)packet_size * L * nd;
+        if (!out || cap_complex < total)
+            throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(total) + " complex values");
+        const cudaStream_t st = h->sim.stream();
+        h->packet.reserve((size_t)total * sizeof(float2), st);
+        h->sim.simulate_packet(packet_size, prt, h->packet.as<float2>(), total);
+        if (cudaMemcpyAsync(out, h->packet.get(), (size_t)total * sizeof(float2), cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            throw SimError(BCSIM_E_CUDA, "packet download failed");
+    });
+}
+
+int bcsim_color_doppler(bcsim_handle* h, const float* iq_packet, int packet_size, int64_t num_lines,
+                        int64_t num_samples, float* r0, float* velocity, const bcsim_scan_geometry* geometry,
+                        uint8_t* bgra) {
+    return guarded(h, [&] {
+        using bcsim_gb300::SimError;
+        if (!iq_packet || num_lines <= 0 || num_samples <= 0) throw SimError(BCSIM_E_INVALID, "No lines returned");
+        if (packet_size < 2) throw SimError(BCSIM_E_INVALID, "a colour-Doppler packet needs at least 2 frames");
+        if (geometry && !bgra) throw SimError(BCSIM_E_INVALID, "null image pointer");
+        const cudaStream_t st = h->sim.stream();
+        const size_t bytes = (size_t)packet_size * num_lines * num_samples * sizeof(float2);
+        h->packet.reserve(bytes, st);
+        if (cudaMemcpyAsync(h->packet.get(), iq_packet, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            throw SimError(BCSIM_E_CUDA, "IQ upload failed");
+        bcsim_gb300::ScanGeometry2D g{};
+        if (geometry) g = to_geometry(geometry);
+        bcsim_gb300::doppler_from_device(st, h->imaging, h->packet.as<float2>(), packet_size, num_lines, num_samples,
+                                         r0, velocity, geometry ? &g : nullptr, bgra);
+    });
+}
+
+int bcsim_simulate_color_doppler(bcsim_handle* h, int packet_size, float prt, float* r0, float* velocity,
+                                 const bcsim_scan_geometry* geometry, uint8_t* bgra) {
+    return guarded(h, [&] {
+        using bcsim_gb300::SimError;
+        if (packet_size < 2) throw SimError(BCSIM_E_INVALID, "a colour-Doppler packet needs at least 2 frames");
+        if (geometry && !bgra) throw SimError(BCSIM_E_INVALID, "null image pointer");
+        int64_t L = 0, nd = 0;
+        h->sim.output_shape(&L, &nd);
+        const int64_t total = (int64_t)packet_size * L * nd;
+        const cudaStream_t st = h->sim.stream();
+        h->packet.reserve((size_t)total * sizeof(float2), st);
+        h->sim.simulate_packet(packet_size, prt, h->packet.as<float2>(), total);
+        bcsim_gb300::ScanGeometry2D g{};
+        if (geometry) g = to_geometry(geometry);
+        bcsim_gb300::doppler_from_device(st, h->imaging, h->packet.as<float2>(), packet_size, L, nd, r0, velocity,
+                                         geometry ? &g : nullptr, bgra);
     });
 }
 

@@ -1311,6 +1311,49 @@ void Simulator::simulate_device(void* dev_out, int64_t cap_complex) {
     simulate(static_cast<float2*>(dev_out), nullptr);
 }
 
+void Simulator::simulate_packet(int P, float prt, float2* dev_out, int64_t cap_complex) {
+    throw_if_not_configured();
+    if (P < 1) throw SimError(BCSIM_E_INVALID, "packet size must be at least 1");
+    int64_t L = 0, nd = 0;
+    output_shape(&L, &nd);
+    const int64_t frame = L * nd;
+    if (!dev_out || cap_complex < (int64_t)P * frame)
+        throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string((int64_t)P * frame) +
+                                              " complex values");
+    ensure_device();
+    if (splines_.empty()) {
+        // fixed scatterers do not move: every frame of the packet is the same
+        simulate(dev_out, nullptr);
+        for (int k = 1; k < P; k++)
+            BCSIM_CUDA(cudaMemcpyAsync(dev_out + k * frame, dev_out, (size_t)frame * sizeof(float2),
+                                       cudaMemcpyDeviceToDevice, stream_));
+    } else {
+        std::vector<float> o((size_t)3 * L), d((size_t)3 * L), l((size_t)3 * L);
+        for (int64_t i = 0; i < L; i++)
+            for (int c = 0; c < 3; c++) {
+                o[3 * i + c] = lines_[i].o[c];
+                d[3 * i + c] = lines_[i].d[c];
+                l[3 * i + c] = lines_[i].l[c];
+            }
+        const std::vector<float> t0 = timestamps_;
+        const float len = line_length_;
+        std::vector<float> t(t0.size());
+        try {
+            for (int k = 0; k < P; k++) {
+                // scanline.get_timestamp() + packet_no * color_prt, in float
+                for (size_t i = 0; i < t.size(); i++) t[i] = t0[i] + (float)k * prt;
+                set_scan_sequence(o.data(), d.data(), l.data(), t.data(), (int)L, len);
+                simulate(dev_out + k * frame, nullptr);
+            }
+        } catch (...) {
+            set_scan_sequence(o.data(), d.data(), l.data(), t0.data(), (int)L, len);
+            throw;
+        }
+        set_scan_sequence(o.data(), d.data(), l.data(), t0.data(), (int)L, len);
+    }
+    check_device_flag();
+}
+
 void Simulator::clone_from(Simulator& o) {
     o.ensure_device();
     ensure_device();

@@ -169,6 +169,10 @@ public:
     void check_device_flag();
     void simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples);
     void simulate_device(void* dev_out, int64_t cap_complex);
+    // A colour-Doppler packet (MainWindow.cpp:664-694): P frames of the scan,
+    // frame k with every line's timestamp advanced by k * prt, into device
+    // memory [P][L][nd].  The scan sequence is restored afterwards.
+    void simulate_packet(int P, float prt, float2* dev_out, int64_t cap_complex);
 
     std::vector<double> get_debug_data(const std::string& key) const;
     void set_logger(LogFn fn, void* user) { log_fn_ = fn; log_user_ = user; }

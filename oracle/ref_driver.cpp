@@ -27,6 +27,8 @@
 #include "utils/GaussPulse.hpp"
 #include "algorithm/CpuAlgorithm.hpp"
 #include "algorithm/common_utils.hpp"
+#include "utils/ScanGeometry.hpp"
+#include "utils/cartesianator/Cartesianator.hpp"
 
 static void copy_err(const char* msg, char* err, int errcap) {
     if (err && errcap > 0) {
@@ -54,6 +56,39 @@ static std::string fstr(float v) {
     char buf[64];
     std::snprintf(buf, sizeof(buf), "%.9g", (double)v);
     return buf;
+}
+
+// The reference's scan converter (CpuCartesianator<T>, src/utils/cartesianator/
+// Cartesianator.cpp:32-205) for a sector (kind 0: width, depth, tilt) or linear
+// (kind 1: width, range_max = depth) geometry; in: [beams][range]; out: [ny][nx].
+template <typename T>
+static int ref_scan_convert_t(const T* in, int beams, int range, int kind, float width, float depth, float tilt,
+                              int nx, int ny, T* out) {
+    try {
+        bcsim::ScanGeometry::ptr g;
+        if (kind == 0) {
+            auto s = std::make_shared<bcsim::SectorScanGeometry>();
+            s->width = width;
+            s->depth = depth;
+            s->tilt = tilt;
+            g = s;
+        } else {
+            auto l = std::make_shared<bcsim::LinearScanGeometry>();
+            l->width = width;
+            l->range_max = depth;
+            g = l;
+        }
+        CpuCartesianator<T> cart;
+        cart.SetGeometry(g);
+        cart.SetOutputSize((size_t)nx, (size_t)ny);
+        std::vector<T> buf(in, in + (size_t)beams * range);
+        cart.Process(buf.data(), beams, range);
+        const T* o = cart.GetOutputBuffer();
+        std::memcpy(out, o, sizeof(T) * (size_t)nx * ny);
+        return 0;
+    } catch (const std::exception&) {
+        return 1;
+    }
 }
 
 extern "C" {
@@ -154,6 +189,16 @@ int ref_uniform_regular_knots(int n, int p, float t0, float t1, float* out, int 
     auto v = bspline_storve::uniform_regular_knot_vector<float>(n, p, t0, t1);
     for (int i = 0; i < (int)v.size() && i < cap; i++) out[i] = v[i];
     return (int)v.size();
+}
+
+int ref_scan_convert_f32(const float* in, int beams, int range, int kind, float width, float depth, float tilt, int nx,
+                         int ny, float* out) {
+    return ref_scan_convert_t(in, beams, range, kind, width, depth, tilt, nx, ny, out);
+}
+
+int ref_scan_convert_u8(const unsigned char* in, int beams, int range, int kind, float width, float depth, float tilt,
+                        int nx, int ny, unsigned char* out) {
+    return ref_scan_convert_t(in, beams, range, kind, width, depth, tilt, nx, ny, out);
 }
 
 }  // extern "C"

@@ -5,6 +5,10 @@
     src/core/unittest/test_fft.cpp:55-90          (fft_conv, next_power_of_two)
     src/core/unittest/test_hilbert_mask.cpp:14-34 (discrete_hilbert_mask)
     src/utils/unittest/test_SignalProcessing.cpp:6-27 (direct_conv)
+* ref_imaging.npz -- seeded float and byte beam spaces, three scan geometries
+  (sector, tilted sector, linear) and what the reference's own scan converter
+  (CpuCartesianator, src/utils/cartesianator/Cartesianator.cpp:107-205)
+  returns for them.
 * ref_<case>.npz -- inputs of a small seeded case, the IQ that the reference's
   own CPU algorithm returns for them (bcsim::Create("cpu")->simulate_lines), and
   the time-projection bins of a few lines from its projection loops
@@ -143,6 +147,28 @@ def arrays_to_job(z) -> W.Job:
 BIN_LINES = (0, 3)
 
 
+IMAGING_GEOMETRIES = [
+    (0, float(np.float32(np.deg2rad(70.0))), 0.12, 0.0, 161, 139),   # sector, 70 degrees, 12 cm
+    (0, 1.0, 0.1, 0.2, 120, 101),                                     # tilted sector
+    (1, 0.04, 0.06, 0.0, 97, 140),                                    # linear, 4 cm x 6 cm
+]
+
+
+def make_imaging():
+    from oracle import imaging as OI
+
+    rng = np.random.default_rng(4242)
+    bf = rng.random((48, 200), dtype=np.float32)
+    bu = (rng.random((48, 200)) * 256).astype(np.uint8)
+    d = {"beamspace_f32": bf, "beamspace_u8": bu, "geometries": np.array(IMAGING_GEOMETRIES, np.float64)}
+    for k, g in enumerate(IMAGING_GEOMETRIES):
+        g = (int(g[0]), g[1], g[2], g[3], int(g[4]), int(g[5]))
+        d[f"ref_f32_{k}"] = OI.ref_scan_convert(bf, g)
+        d[f"ref_u8_{k}"] = OI.ref_scan_convert(bu, g)
+    np.savez_compressed(os.path.join(HERE, "ref_imaging.npz"), **d)
+    print("imaging", os.path.getsize(os.path.join(HERE, "ref_imaging.npz")))
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libbcsim_ref.so is missing: run `make -C oracle all` where the reference sources are")
@@ -160,4 +186,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["imaging"]:
+        make_imaging()
+    else:
+        main()
+        make_imaging()
