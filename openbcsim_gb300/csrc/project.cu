@@ -26,6 +26,7 @@
 // where the reference's GPU path (cuda_kernels_fixed.cuh:59-62) uses float
 // atomics whose order varies from run to run.
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <cub/device/device_radix_sort.cuh>
 #include "kernels.hpp"
@@ -474,6 +475,37 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
 
     const int stride = PD ? 2 : 1;
     const float scale = p.scale;
+    // Do the staged planes hold every record's radial plane?  Then the walk
+    // reads the table from shared memory without a per-record check, and each
+    // record carries its plane's offset in shared memory (in B.z).
+    __shared__ int s_r0_min, s_r0_max;
+    bool all_staged = false;
+    if (BEAM == BEAM_LUT && !REF && lut_staged > 0) {
+        if (tid == 0) {
+            s_r0_min = 0x7fffffff;
+            s_r0_max = -0x7fffffff;
+        }
+        __syncthreads();
+        int mn = 0x7fffffff, mx = -0x7fffffff;
+        for (int r = tid; r < cnt; r += blockDim.x) {
+            const int r0 = __float_as_int(smB[r].z);
+            mn = min(mn, r0);
+            mx = max(mx, r0);
+        }
+        mn = __reduce_min_sync(0xffffffffu, mn);
+        mx = __reduce_max_sync(0xffffffffu, mx);
+        if (lane == 0) {
+            atomicMin(&s_r0_min, mn);
+            atomicMax(&s_r0_max, mx);
+        }
+        __syncthreads();
+        all_staged = s_r0_min >= lut_base && s_r0_max < lut_base + lut_staged;
+        if (all_staged) {
+            for (int r = tid; r < cnt; r += blockDim.x)
+                smB[r].z = __int_as_float((__float_as_int(smB[r].z) - lut_base) * lut_splane);
+            __syncthreads();
+        }
+    }
     const int first_bin = __float_as_int(smB[0].w);
     const int last_bin = __float_as_int(smB[cnt - 1].w);
     // lookup-table coordinate ranges -1 < t < n-1 as |t - c| < h
@@ -518,6 +550,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
 
         // ---- phase A: records this warp's lines can see ----
         unsigned mask = 0xffffffffu;
+        bool front_certain = false;
         if (cull) {
             const SlotCone* c = cones + min(g0 + (tid & ~31), L - 1) / 32;   // warp-uniform
             const float lx = __ldg(&c->lx), ly = __ldg(&c->ly), lz = __ldg(&c->lz);
@@ -526,9 +559,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             const float du_par = __ldg(&c->du_par), du_perp = __ldg(&c->du_perp);
             const float dv_par = __ldg(&c->dv_par), dv_perp = __ldg(&c->dv_perp), dd = __ldg(&c->dd);
             mask = 0;
+            bool certain = true;   // every selected record in front of every line of the slot
             for (int w = 0; w < nwords; w++) {
                 const int r = (w << 5) + lane;
-                bool pass = false;
+                bool pass = false, sure = true;
                 if (r < cnt) {
                     const float4 A = smA[r];
                     const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
@@ -547,10 +581,16 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     const bool front = dt >= 0.0f || fmaf(dt, dt, ap2) * (dd * dd) >= dt * dt;
                     pass = (u + su > p.cull_l_lo) && (u - su < p.cull_l_hi) && (v + sv > p.cull_e_lo) &&
                            (v - sv < p.cull_e_hi) && front;
+                    // every line's A.r_k >= dt - |A| dd: in front of all of them, with a
+                    // margin of 1e-5 |A| for the rounding of the per-pair dot product
+                    const float ddm = dd + 1e-5f;
+                    sure = !pass || (dt > 0.0f && dt * dt > fmaf(dt, dt, ap2) * (ddm * ddm) * 1.0001f);
                 }
                 const unsigned m = __ballot_sync(0xffffffffu, pass);
+                certain = certain && __all_sync(0xffffffffu, sure);
                 if (lane == w) mask = m;
             }
+            front_certain = certain;
         }
 
         // ---- phase B: walk the selected records in order ----
@@ -582,104 +622,121 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 }
             }
         };
-        while (nz) {
-            const int w = __ffs(nz) - 1;
-            nz &= nz - 1u;
-            unsigned word = __shfl_sync(0xffffffffu, mask_w, w);
-            while (word) {
-                const int i = (w << 5) + __ffs(word) - 1;
-                word &= word - 1u;
-                const float4 B = smB[i];
-                const float4 A = smA[i];
-                if (i >= seg_end) {   // warp-uniform
-                    tr += f2ll_rn(ar * scale);
-                    if (PD) ti += f2ll_rn(ai * scale);
-                    ar = 0.0f;
-                    ai = 0.0f;
-                    do { sg++; } while (s_seg[sg + 1] <= i);
-                    seg_end = s_seg[sg + 1];
-                    const int nb = __float_as_int(B.w);
-                    if (nb != cur) {
-                        store_bin();
-                        tr = 0;
-                        ti = 0;
-                        cur = nb;
-                    }
-                }
-                float w8;
-                if (REF) {
-                    // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
-                    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
-                    const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
-                    const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
-                    if (BEAM == BEAM_GAUSSIAN) {
-                        w8 = gauss_weight_ref(b, l, e);
-                    } else {
-                        // the reference recomputes the radial table coordinate per pair from r
-                        w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
-                                                                   __fmul_rn(A.z, A.z))),
-                                            l, e);
-                    }
-                    w8 = signbit(dot) ? 0.0f : w8;
-                } else {
-                    const float dot = fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
-                    const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
-                    const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
-                    if (BEAM == BEAM_GAUSSIAN) {
-                        w8 = exp2f(-fmaf(u, u, v * v));
-                        // arc projection: a line for which the scatterer lies behind the
-                        // origin sees it at -rho, outside [0, ns) for every record
-                        // (near-origin scatterers take the per-pair path)
-                        w8 = signbit(dot) ? 0.0f : w8;
-                    } else {
-                        w8 = 0.0f;
-                        // (a warp whose lanes all miss the table skips the lookup)
-                        if (fabsf(u - cl) < hl && fabsf(v - ce) < he && !signbit(dot)) {
-                            // -1 < t < n-1: the reference's trunc-toward-zero index
-                            // with the fraction dropped for -1 < t < 0
-                            // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
-                            // integer part of max(t, 0) + 2^23 rounded down
-                            // (paired FP32 operations, two per instruction; the same
-                            // rounding per component as the scalar forms)
-                            const float2 ucv = make_float2(fmaxf(u, 0.0f), fmaxf(v, 0.0f));
-                            const float2 t2 = __fadd2_rd(ucv, make_float2(8388608.0f, 8388608.0f));
-                            const int l0 = __float_as_int(t2.x) - 0x4B000000, e0 = __float_as_int(t2.y) - 0x4B000000;
-                            // fraction = t - floor(t): uc - (tu - 2^23), both differences exact
-                            const float2 fle = __ffma2_rn(__fadd2_rn(t2, make_float2(-8388608.0f, -8388608.0f)),
-                                                          make_float2(-1.0f, -1.0f), ucv);
-                            const float fl = fle.x, fe = fle.y;
-                            const int r0 = __float_as_int(B.z);
-                            float4 P, Q;
-                            if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
-                                const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
-                                P = pl[0];
-                                Q = pl[lut_row];
-                            } else {
-                                const int base = r0 * lut_plane_size + l0 * b.ne + e0;
-                                P = __ldg(b.lut4 + base);
-                                Q = __ldg(b.lut4 + base + b.ne);
-                            }
-                            const float fr = B.y;
-                            // radial (the table holds the radial differences),
-                            // lateral, elevational (BeamProfile.cpp:116-127)
-                            // (c00, c01) and (c10, c11), then (c0, c1) = c.0 + fl (c.1 - c.0)
-                            const float2 frr = make_float2(fr, fr);
-                            const float2 cl0 = __ffma2_rn(frr, make_float2(P.z, P.w), make_float2(P.x, P.y));
-                            const float2 cl1 = __ffma2_rn(frr, make_float2(Q.z, Q.w), make_float2(Q.x, Q.y));
-                            const float2 dl = __ffma2_rn(cl0, make_float2(-1.0f, -1.0f), cl1);
-                            const float2 ce2 = __ffma2_rn(make_float2(fl, fl), dl, cl0);
-                            w8 = fmaf(fe, ce2.y - ce2.x, ce2.x);
+        auto walk = [&](auto nodot_tag, auto staged_tag) {
+            constexpr bool NODOT = decltype(nodot_tag)::value;
+            constexpr bool STAGED = decltype(staged_tag)::value;
+            while (nz) {
+                const int w = __ffs(nz) - 1;
+                nz &= nz - 1u;
+                unsigned word = __shfl_sync(0xffffffffu, mask_w, w);
+                while (word) {
+                    const int i = (w << 5) + __ffs(word) - 1;
+                    word &= word - 1u;
+                    const float4 B = smB[i];
+                    const float4 A = smA[i];
+                    if (i >= seg_end) {   // warp-uniform
+                        tr += f2ll_rn(ar * scale);
+                        if (PD) ti += f2ll_rn(ai * scale);
+                        ar = 0.0f;
+                        ai = 0.0f;
+                        do { sg++; } while (s_seg[sg + 1] <= i);
+                        seg_end = s_seg[sg + 1];
+                        const int nb = __float_as_int(B.w);
+                        if (nb != cur) {
+                            store_bin();
+                            tr = 0;
+                            ti = 0;
+                            cur = nb;
                         }
                     }
-                }
-                ar = fmaf(w8, A.w, ar);
-                if (PD) ai = fmaf(w8, B.x, ai);
-                if (COUNT) {
-                    walked += active ? 1u : 0u;
-                    weighted += (active && w8 != 0.0f) ? 1u : 0u;
-                    idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
+                    float w8;
+                    if (REF) {
+                        // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
+                        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.rx), __fmul_rn(A.y, q.ry)), __fmul_rn(A.z, q.rz));
+                        const float l = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.ux), __fmul_rn(A.y, q.uy)), __fmul_rn(A.z, q.uz));
+                        const float e = __fadd_rn(__fadd_rn(__fmul_rn(A.x, q.vx), __fmul_rn(A.y, q.vy)), __fmul_rn(A.z, q.vz));
+                        if (BEAM == BEAM_GAUSSIAN) {
+                            w8 = gauss_weight_ref(b, l, e);
+                        } else {
+                            // the reference recomputes the radial table coordinate per pair from r
+                            w8 = lut_weight_ref(b, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(A.x, A.x), __fmul_rn(A.y, A.y)),
+                                                                       __fmul_rn(A.z, A.z))),
+                                                l, e);
+                        }
+                        w8 = signbit(dot) ? 0.0f : w8;
+                    } else {
+                        const float dot = NODOT ? 1.0f : fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
+                        const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
+                        const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
+                        if (BEAM == BEAM_GAUSSIAN) {
+                            w8 = exp2f(-fmaf(u, u, v * v));
+                            // arc projection: a line for which the scatterer lies behind the
+                            // origin sees it at -rho, outside [0, ns) for every record
+                            // (near-origin scatterers take the per-pair path)
+                            if (!NODOT) w8 = signbit(dot) ? 0.0f : w8;
+                        } else {
+                            w8 = 0.0f;
+                            // (a warp whose lanes all miss the table skips the lookup)
+                            if (fabsf(u - cl) < hl && fabsf(v - ce) < he && (NODOT || !signbit(dot))) {
+                                // -1 < t < n-1: the reference's trunc-toward-zero index
+                                // with the fraction dropped for -1 < t < 0
+                                // (BeamProfile.cpp:94-103) is floor(max(t, 0)), the
+                                // integer part of max(t, 0) + 2^23 rounded down
+                                // (paired FP32 operations, two per instruction; the same
+                                // rounding per component as the scalar forms)
+                                const float2 ucv = make_float2(fmaxf(u, 0.0f), fmaxf(v, 0.0f));
+                                const float2 t2 = __fadd2_rd(ucv, make_float2(8388608.0f, 8388608.0f));
+                                const int l0 = __float_as_int(t2.x) - 0x4B000000, e0 = __float_as_int(t2.y) - 0x4B000000;
+                                // fraction = t - floor(t): uc - (tu - 2^23), both differences exact
+                                const float2 fle = __ffma2_rn(__fadd2_rn(t2, make_float2(-8388608.0f, -8388608.0f)),
+                                                              make_float2(-1.0f, -1.0f), ucv);
+                                const float fl = fle.x, fe = fle.y;
+                                const int r0 = __float_as_int(B.z);
+                                float4 P, Q;
+                                if (STAGED) {   // B.z holds the record's plane offset in shared memory
+                                    const float4* pl = smL + r0 + l0 * lut_row + e0;
+                                    P = pl[0];
+                                    Q = pl[lut_row];
+                                } else if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
+                                    const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
+                                    P = pl[0];
+                                    Q = pl[lut_row];
+                                } else {
+                                    const int base = r0 * lut_plane_size + l0 * b.ne + e0;
+                                    P = __ldg(b.lut4 + base);
+                                    Q = __ldg(b.lut4 + base + b.ne);
+                                }
+                                const float fr = B.y;
+                                // radial (the table holds the radial differences),
+                                // lateral, elevational (BeamProfile.cpp:116-127)
+                                // (c00, c01) and (c10, c11), then (c0, c1) = c.0 + fl (c.1 - c.0)
+                                const float2 frr = make_float2(fr, fr);
+                                const float2 cl0 = __ffma2_rn(frr, make_float2(P.z, P.w), make_float2(P.x, P.y));
+                                const float2 cl1 = __ffma2_rn(frr, make_float2(Q.z, Q.w), make_float2(Q.x, Q.y));
+                                const float2 dl = __ffma2_rn(cl0, make_float2(-1.0f, -1.0f), cl1);
+                                const float2 ce2 = __ffma2_rn(make_float2(fl, fl), dl, cl0);
+                                w8 = fmaf(fe, ce2.y - ce2.x, ce2.x);
+                            }
+                        }
+                    }
+                    ar = fmaf(w8, A.w, ar);
+                    if (PD) ai = fmaf(w8, B.x, ai);
+                    if (COUNT) {
+                        walked += active ? 1u : 0u;
+                        weighted += (active && w8 != 0.0f) ? 1u : 0u;
+                        idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
+                    }
                 }
             }
+        };
+        using T_ = std::true_type;
+        using F_ = std::false_type;
+        if (!REF && front_certain) {
+            if (BEAM == BEAM_LUT && all_staged) walk(T_{}, T_{});
+            else walk(T_{}, F_{});
+        } else {
+            if (BEAM == BEAM_LUT && !REF && all_staged) walk(F_{}, T_{});
+            else walk(F_{}, F_{});
         }
         tr += f2ll_rn(ar * scale);
         if (PD) ti += f2ll_rn(ai * scale);
