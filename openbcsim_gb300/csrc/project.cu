@@ -558,6 +558,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             const float rx = __ldg(&c->rx), ry = __ldg(&c->ry), rz = __ldg(&c->rz);
             const float du_par = __ldg(&c->du_par), du_perp = __ldg(&c->du_perp);
             const float dv_par = __ldg(&c->dv_par), dv_perp = __ldg(&c->dv_perp), dd = __ldg(&c->dd);
+            const float dd2 = dd * dd * 1.0001f + 1e-12f;
+            const float ddm2 = (dd + 1e-5f) * (dd + 1e-5f) * 1.0001f;
+            const float cl_c = 0.5f * (p.cull_l_lo + p.cull_l_hi), ce_c = 0.5f * (p.cull_e_lo + p.cull_e_hi);
+            const float cl_h = 0.5f * (p.cull_l_hi - p.cull_l_lo) + 1e-6f * (fabsf(p.cull_l_lo) + fabsf(p.cull_l_hi));
+            const float ce_h = 0.5f * (p.cull_e_hi - p.cull_e_lo) + 1e-6f * (fabsf(p.cull_e_lo) + fabsf(p.cull_e_hi));
             mask = 0;
             bool certain = true;   // every selected record in front of every line of the slot
             for (int w = 0; w < nwords; w++) {
@@ -568,23 +573,21 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
                     const float v = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
                     const float dt = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
-                    // |A_perp|^2 = |A x r|^2 (no cancellation for A along r); |A_perp|
-                    // bounded from above (rsqrt's error is far below 1e-5)
-                    const float cx = fmaf(A.y, rz, -A.z * ry), cy = fmaf(A.z, rx, -A.x * rz);
-                    const float cz = fmaf(A.x, ry, -A.y * rx);
-                    const float ap2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+                    // |A|^2, and |A_perp|^2 = |A|^2 - dt^2 bounded from above: the
+                    // margin 4e-6 |A|^2 exceeds the rounding of both terms and of the
+                    // slot axis' length (rsqrt's error is far below 1e-5)
+                    const float a2 = fmaf(A.z, A.z, fmaf(A.y, A.y, A.x * A.x));
+                    const float ap2 = fmaf(a2, 4e-6f, fmaxf(fmaf(-dt, dt, a2), 0.0f));
                     const float ap = ap2 * rsqrtf(fmaxf(ap2, 1e-30f)) * 1.00001f;
                     const float adt = fabsf(dt);
                     const float su = fmaf(adt, du_par, ap * du_perp), sv = fmaf(adt, dv_par, ap * dv_perp);
-                    // some line may have the record in front: A.r_k >= dt - |A| dd,
-                    // with |A|^2 = dt^2 + |A_perp|^2
-                    const bool front = dt >= 0.0f || fmaf(dt, dt, ap2) * (dd * dd) >= dt * dt;
-                    pass = (u + su > p.cull_l_lo) && (u - su < p.cull_l_hi) && (v + sv > p.cull_e_lo) &&
-                           (v - sv < p.cull_e_hi) && front;
+                    // some line may have the record in front: A.r_k >= dt - |A| dd
+                    const bool front = dt >= 0.0f || a2 * dd2 >= dt * dt;
+                    // lo - s < u < hi + s as |u - c| < h + s (h widened past the roundings)
+                    pass = fabsf(u - cl_c) < cl_h + su && fabsf(v - ce_c) < ce_h + sv && front;
                     // every line's A.r_k >= dt - |A| dd: in front of all of them, with a
                     // margin of 1e-5 |A| for the rounding of the per-pair dot product
-                    const float ddm = dd + 1e-5f;
-                    sure = !pass || (dt > 0.0f && dt * dt > fmaf(dt, dt, ap2) * (ddm * ddm) * 1.0001f);
+                    sure = !pass || (dt > 0.0f && dt * dt > a2 * ddm2);
                 }
                 const unsigned m = __ballot_sync(0xffffffffu, pass);
                 certain = certain && __all_sync(0xffffffffu, sure);
