@@ -88,7 +88,9 @@ static std::string fmt_double(double v) {
 
 Simulator::Simulator() = default;
 
-Simulator::~Simulator() = default;   // buffers freed in stream order, then the stream (OwnedStream)
+Simulator::~Simulator() {   // buffers freed in stream order, then the streams (OwnedStream)
+    for (cudaEvent_t e : ev_blocks_) cudaEventDestroy(e);
+}
 
 void Simulator::log(int level, const std::string& msg) const {
     if (log_fn_) log_fn_(level, msg.c_str(), log_user_);
@@ -101,6 +103,11 @@ void Simulator::ensure_device() {
     if (device_ < 0 || device_ >= count) throw SimError(BCSIM_E_INVALID, "illegal CUDA device number");
     BCSIM_CUDA(cudaSetDevice(device_));
     BCSIM_CUDA(cudaStreamCreateWithFlags(&owned_stream_.s, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&side_stream_.s, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&copy_stream_.s, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaEventCreateWithFlags(&ev_fork_.e, cudaEventDisableTiming));
+    BCSIM_CUDA(cudaEventCreateWithFlags(&ev_join_.e, cudaEventDisableTiming));
+    BCSIM_CUDA(cudaEventCreateWithFlags(&ev_copied_.e, cudaEventDisableTiming));
     stream_ = owned_stream_.s;
     device_ready_ = true;
     {
@@ -1087,7 +1094,7 @@ void Simulator::prepare() {
 // ---------------------------------------------------------------------------
 // enqueue: device work only (capturable: no allocation, no host copy, no sync)
 // ---------------------------------------------------------------------------
-void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
+void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out) {
     const Plan& P = plan_;
     const SimParams& p = P.p;
     const BeamDev& b = P.b;
@@ -1098,13 +1105,29 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     unsigned long long* bins = bins_.as<unsigned long long>();
     int launches = 0;   // kernels of this library launched (the radix sort's are counted apart)
     const LineGeom* lines_d = lines_dev_.as<LineGeom>();
-    BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, st));
+    // the bins are cleared on the side stream, after st's earlier work (the
+    // previous convolution read them), while the records are prepared; st
+    // waits for it before the first kernel that writes bins
+    {
+        const cudaStream_t side = side_stream_.s;
+        EventTimer mt(timing, side);
+        BCSIM_CUDA(cudaEventRecord(ev_fork_.e, st));
+        BCSIM_CUDA(cudaStreamWaitEvent(side, ev_fork_.e, 0));
+        if (timing) mt.restart();
+        BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, side));
+        BCSIM_CUDA(cudaEventRecord(ev_join_.e, side));
+        if (timing) debug_["kernel_memset_ms"].push_back(mt.stop());
+    }
+    bool joined = false;
+    auto join_bins = [&]() {
+        if (!joined) BCSIM_CUDA(cudaStreamWaitEvent(st, ev_join_.e, 0));
+        joined = true;
+    };
     unsigned long long* pair_counts = nullptr;   // instrumented run (count_pairs)
     if (count_pairs_ && p.mode == MODE_FP64) {
         pair_counts = pair_counts_.as<unsigned long long>();
         BCSIM_CUDA(cudaMemsetAsync(pair_counts, 0, 4 * sizeof(unsigned long long), st));
     }
-    if (timing) debug_["kernel_memset_ms"].push_back(timer.stop());
 
     if (P.n_shared > 0) {
         const int64_t N = P.n_shared;
@@ -1138,6 +1161,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
         if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
         timer.restart();
 
+        join_bins();
         ++launches;
         BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
                                          line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins,
@@ -1166,6 +1190,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     }
 
     // per-pair path
+    join_bins();
     timer.restart();
     for (const GenLaunch& g : P.gl) {
         if (g.kind == 0) {
@@ -1189,13 +1214,37 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing) {
     }
     if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
 
-    // convolution + demodulation + decimation
+    // convolution + demodulation + decimation; with a host destination in
+    // blocks of lines, each block's IQ copied out while the next is convolved
     timer.restart();
-    ++launches;
-    BCSIM_CUDA(launch_convolve_demodulate(bins, L, ns, p.phase_delay, std::ldexp(1.0f, -p.log2scale),
-                                          taps_pm_dev_.as<float2>(), ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_,
-                                          (int)tap_count_, (int)tap_start_, M_, center_, decimation_, (int)nd_,
-                                          demod_dev_.as<float2>(), dev_out, st));
+    const int nblocks = (host_out && L >= 1024) ? 4 : 1;
+    while ((int)ev_blocks_.size() < nblocks) {
+        cudaEvent_t e = nullptr;
+        BCSIM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_blocks_.push_back(e);
+    }
+    const int stride_bins = p.phase_delay ? 2 : 1;
+    for (int k = 0; k < nblocks; k++) {
+        const int l0 = (int)((int64_t)L * k / nblocks), l1 = (int)((int64_t)L * (k + 1) / nblocks);
+        if (l1 <= l0) continue;
+        ++launches;
+        BCSIM_CUDA(launch_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns, p.phase_delay,
+                                              std::ldexp(1.0f, -p.log2scale), taps_pm_dev_.as<float2>(),
+                                              ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_, (int)tap_count_,
+                                              (int)tap_start_, M_, center_, decimation_, (int)nd_,
+                                              demod_dev_.as<float2>(), dev_out + (int64_t)l0 * nd_, st));
+        if (host_out) {
+            const cudaStream_t cs = copy_stream_.s;
+            BCSIM_CUDA(cudaEventRecord(ev_blocks_[k], st));
+            BCSIM_CUDA(cudaStreamWaitEvent(cs, ev_blocks_[k], 0));
+            BCSIM_CUDA(cudaMemcpyAsync(host_out + 2 * (int64_t)l0 * nd_, dev_out + (int64_t)l0 * nd_,
+                                       (size_t)(l1 - l0) * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, cs));
+        }
+    }
+    if (host_out) {
+        BCSIM_CUDA(cudaEventRecord(ev_copied_.e, copy_stream_.s));
+        BCSIM_CUDA(cudaStreamWaitEvent(st, ev_copied_.e, 0));
+    }
     if (timing) {
         debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
         debug_["total_ms"].push_back(total.stop());
@@ -1207,7 +1256,7 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     prepare();
     if (store_details_) debug_.clear();
     const cudaStream_t st = stream_;
-    enqueue(st, dev_out, store_details_);
+    enqueue(st, dev_out, store_details_, host_out);
     if (count_pairs_ && mode_ == MODE_FP64) {
         unsigned long long c[4] = {0, 0, 0, 0};
         BCSIM_CUDA(cudaMemcpyAsync(c, pair_counts_.get(), sizeof c, cudaMemcpyDeviceToHost, st));
@@ -1219,7 +1268,7 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
     }
     if (host_out) {
         EventTimer timer(store_details_, st);
-        BCSIM_CUDA(cudaMemcpyAsync(host_out, dev_out, (size_t)num_lines_ * nd_ * sizeof(float2), cudaMemcpyDeviceToHost, st));
+        // (the IQ was copied by enqueue, overlapped with the convolution)
         // the bounded-wait error flag travels with the result (one synchronisation)
         if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
         BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, st));

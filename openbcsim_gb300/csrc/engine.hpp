@@ -123,6 +123,17 @@ struct Plan {
     uint64_t records_key = 0;
 };
 
+// An event without timing, destroyed with its owner.
+struct OwnedEvent {
+    cudaEvent_t e = nullptr;
+    OwnedEvent() = default;
+    OwnedEvent(const OwnedEvent&) = delete;
+    OwnedEvent& operator=(const OwnedEvent&) = delete;
+    ~OwnedEvent() {
+        if (e) cudaEventDestroy(e);
+    }
+};
+
 class Simulator {
 public:
     Simulator();
@@ -150,9 +161,12 @@ public:
     // Host work of simulate_lines for the current configuration (cached).
     void prepare();
     // Device work of simulate_lines on stream st into dev_out: launches only,
-    // no allocation, no host copy, no synchronisation (can be graph-captured
-    // after prepare()).
-    void enqueue(cudaStream_t st, float2* dev_out, bool timing);
+    // no allocation, no synchronisation (can be graph-captured after
+    // prepare()).  With host_out (pinned or pageable host memory), the
+    // convolution runs in blocks of lines and each block's IQ is copied to
+    // host_out on a copy stream while the next block is convolved; st then
+    // waits for the copies.
+    void enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out = nullptr);
     // Copy the whole configuration of o (parameters, excitation, beam, scatterer
     // datasets -- device copies; not the scan sequence) into this simulator.
     void clone_from(Simulator& o);
@@ -194,6 +208,10 @@ private:
     int device_ = 0;
     bool device_ready_ = false;
     OwnedStream owned_stream_;
+    OwnedStream side_stream_;   // bins cleared here while the records are prepared
+    OwnedStream copy_stream_;   // IQ copied to the host here while later lines are convolved
+    OwnedEvent ev_fork_, ev_join_, ev_copied_;
+    std::vector<cudaEvent_t> ev_blocks_;   // one per convolution block (owned, see ~Simulator)
     PinnedInt flag_host_;
     cudaStream_t stream_ = nullptr;   // owned_stream_.s
     int verbose_ = 0;
