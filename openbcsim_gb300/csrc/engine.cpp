@@ -1076,10 +1076,12 @@ void Simulator::prepare() {
                                     vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
         sort_tmp_.reserve(tmp_bytes, stream_);
         P.sort_tmp_bytes = tmp_bytes;
-        // records per CTA (a multiple of 128 so that results do not depend on it):
-        // enough CTAs to fill the GPU several times over
+        // records per CTA: enough CTAs to fill the GPU several times over, a
+        // multiple of the fold group (512 records when chunks of 512 fill the
+        // GPU, else 128), so that results do not depend on the chunk
+        P.p.fold = (N + 511) / 512 >= 4 * 152 ? 512 : 128;
         int chunk = 1024;
-        while (chunk > 128 && (N + chunk - 1) / chunk < 4 * 152) chunk /= 2;
+        while (chunk > P.p.fold && (N + chunk - 1) / chunk < 4 * 152) chunk /= 2;
         P.chunk = chunk;
         P.records_key = records_key_of(P);
     }
@@ -1307,7 +1309,7 @@ void Simulator::autotune() {
         }
     }
     std::vector<int> chunks = {P.chunk};
-    if (P.n_shared > 0) chunks = {128, 256, 512, 1024};
+    if (P.n_shared > 0) chunks = P.p.fold == 512 ? std::vector<int>{512, 1024} : std::vector<int>{128, 256, 512, 1024};
     const cudaStream_t st = stream_;
     out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2), stream_);
     cudaEvent_t e0, e1;

@@ -55,6 +55,7 @@ struct SimParams {
     float cull_rho_per_bin;    // upper bound of 1 / (2 fs / c)
     int wide_cta;              // shared-origin kernel: 1024/512-thread CTAs for >= 512 lines
     int lut_smem;              // wide shared-origin kernel: lookup-table planes in shared memory
+    int fold;                  // shared-origin kernel: FP32 run sums folded at record indices k*fold (power of 2)
 };
 
 // Frame spread of a slot of 32 lines (consecutive in the kernel's line order):

@@ -356,9 +356,10 @@ __global__ void gather_records_kernel(const uint32_t* __restrict__ svals, const 
 // ---------------------------------------------------------------------------
 __device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
 
-// Records per folding of the FP32 run sum into the integer bin total: bounds
-// the length of any FP32 summation to FOLD terms.
-constexpr int FOLD = 128;
+// The FP32 run sum of a line is folded into its integer bin total at absolute
+// record indices k * p.fold (128 or 512, fixed per configuration; chunks are
+// multiples of it), which bounds any FP32 summation to p.fold terms and keeps
+// the result independent of the chunk size.
 
 // Per-line constants of the shared-origin kernel (fp64 mode):
 //   Gaussian: u = lateral * sqrt(gl), v = elevational * sqrt(ge), so that the
@@ -403,7 +404,7 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
 //      ballot word per 32 records, word w kept by lane w.
 //   B. walk: only the records whose bit is set, in bin order.  A line's
 //      contributions to one bin are summed in FP32, folded into an int64 total
-//      at absolute record indices k*FOLD, and written when the bin changes: a
+//      at absolute record indices k*p.fold, and written when the bin changes: a
 //      plain store for bins strictly inside the chunk (no other CTA holds
 //      records there), an integer atomic for the chunk's first and last bin.
 // Skipped records contribute exactly 0, so the result is bit-identical to
@@ -521,7 +522,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         int total = 0;
         for (int base = 0; base < cnt; base += blockDim.x) {
             const int r = base + tid;
-            const bool start = r < cnt && (r == 0 || (r % FOLD) == 0 ||
+            const bool start = r < cnt && (r == 0 || (r & (p.fold - 1)) == 0 ||
                                            __float_as_int(smB[r].w) != __float_as_int(smB[r - 1].w));
             const unsigned bal = __ballot_sync(0xffffffffu, start);
             if (lane == 0) s_seg_warp[wid] = __popc(bal);
@@ -1143,7 +1144,7 @@ static cudaError_t launch_shared_t(const float4* records, int64_t plane, const i
                                    const LineGeom* lines, const int* line_order, const SlotCone* cones, int L,
                                    const SimParams& p, const BeamDev& b, unsigned long long* bins,
                                    unsigned long long* pair_counts, cudaStream_t stream) {
-    if (chunk > 1024 || chunk % FOLD) return cudaErrorInvalidValue;
+    if (chunk > 1024 || p.fold < 1 || (p.fold & (p.fold - 1)) || chunk % p.fold) return cudaErrorInvalidValue;
     size_t smem = 2 * (size_t)chunk * sizeof(float4);
     const int64_t chunks = (n + chunk - 1) / chunk;
     if (p.wide_cta && L >= 512) {
