@@ -34,11 +34,16 @@
 // flight per thread), convert them and store the phase rows; while one CTA
 // convolves, the SM's other resident CTAs load theirs.
 //
-// Complex MACs use three real products (Gauss): for bin a + ib and tap c + id,
-//     k1 += c (a + b),   (k2, k3) += (a (d - c), b (c + d))   (one FFMA2),
-//     re = k1 - k3,  im = k1 + k2,
-// three FMA-pipe lane operations per complex MAC instead of four.
+// Complex MACs split the analytic pulse h_a = h + i g by parts.  Its real part
+// is the excitation itself (Re IFFT(FFT(h) mask) = h for the Hilbert mask), so
+// h is non-zero only on the excitation's short support, while g (the Hilbert
+// transform) fills the window.  For bin a + ib,
+//     G += (a, b) g  over every tap,  H += (a, b) h  over the support only,
+//     y = (H.re - G.im, H.im + G.re),
+// each a paired FP32 FMA (FFMA2) per tap and output: one per complex MAC
+// outside the support, two inside it.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "kernels.hpp"
@@ -52,10 +57,10 @@ constexpr int CONV_K = 4;   // outputs per thread
 __device__ __forceinline__ void rmac(float2& y, float2 v, float4 h) {
     y = __ffma2_rn(make_float2(v.x, v.x), make_float2(h.x, h.y), y);
 }
-// tap c + id in the form the MAC loop reads: (d - c, c + d, c, 0) for complex
-// bins (Gauss), (c, d, 0, 0) for real bins
-__device__ __forceinline__ float4 tap_gauss(float2 h) { return make_float4(h.y - h.x, h.x + h.y, h.x, 0.0f); }
-__device__ __forceinline__ float4 tap_real(float2 h) { return make_float4(h.x, h.y, 0.0f, 0.0f); }
+// tap h + ig in the form the MAC loop reads: (g, g, h, h) for complex bins,
+// (h, g, 0, 0) for real bins
+__device__ __forceinline__ float4 tap_split(float2 t) { return make_float4(t.y, t.y, t.x, t.x); }
+__device__ __forceinline__ float4 tap_real(float2 t) { return make_float4(t.x, t.y, 0.0f, 0.0f); }
 
 // Fixed-point bin -> float (times inv_scale = 2^-S).  The magnitude is split
 // as hi * 2^32 + lo; hi * 2^32 + float(lo) is rounded once by the FMA and
@@ -77,7 +82,8 @@ __host__ __device__ __forceinline__ int conv_rowpad(int sub) { return ((2 - 4 * 
 // The MAC loop of one thread: outputs 4*tid .. 4*tid+3 of the staged item, over
 // all D phases.  seg: [D][row] with 4 sub-rows of `sub` positions per row;
 // tp4: taps in shared memory (TAPS_SMEM) else taps_pm in global memory;
-// ph: phase offsets into the phase-major taps (D + 1 entries).
+// ph: phase offsets into the phase-major taps (D + 1 entries), then per phase
+// the range [lo, hi) of 4-tap iterations that hold the excitation's support.
 //
 // Iteration i of a phase covers taps 4i .. 4i+3: it needs row elements
 // r0[i], r1[i], r2[i] (from iteration i-1), r3[i], r0[i+1], r1[i+1], r2[i+1]
@@ -87,15 +93,15 @@ __host__ __device__ __forceinline__ int conv_rowpad(int sub) { return ((2 - 4 * 
 // shared-memory load has a whole iteration to land, with no register moves.
 struct FirSet {
     float2 a, b, c, d;        // r3[i], r0[i+1], r1[i+1], r2[i+1]
-    float sa, sb, sc, sd;     // their re + im (complex bins)
     float4 h0, h1, h2, h3;    // taps 4i .. 4i+3
 };
 
 template <bool PD, bool TAPS_SMEM>
 __device__ __forceinline__ void fir_mac(const float2* seg, int row, int sub, int tid, const float4* tp4,
                                         const float2* __restrict__ taps_pm, const int* ph, int D, float2 out[4]) {
-    float2 y0 = make_float2(0.f, 0.f), y1 = y0, y2 = y0, y3 = y0;
-    float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
+    // PD: G (every tap) and H (support taps); real bins: y in G
+    float2 G0 = make_float2(0.f, 0.f), G1 = G0, G2 = G0, G3 = G0;
+    float2 H0 = G0, H1 = G0, H2 = G0, H3 = G0;
     for (int p = 0; p < D; p++) {
         // element tid*4 + t + j of the phase row: sub-row j & 3, position tid + t/4 + j/4
         const float2* r0 = seg + p * row + tid;
@@ -105,10 +111,11 @@ __device__ __forceinline__ void fir_mac(const float2* seg, int row, int sub, int
         const int t_beg = ph[p];
         const int n4 = (ph[p + 1] - t_beg) >> 2;
         if (n4 == 0) continue;
+        const int h_lo = ph[D + 1 + 2 * p], h_hi = ph[D + 2 + 2 * p];
         const float4* hp = tp4 + t_beg;
         const float2* hg = taps_pm + t_beg;
         auto tap = [&](int t) -> float4 {
-            return TAPS_SMEM ? hp[t] : (PD ? tap_gauss(__ldg(hg + t)) : tap_real(__ldg(hg + t)));
+            return TAPS_SMEM ? hp[t] : (PD ? tap_split(__ldg(hg + t)) : tap_real(__ldg(hg + t)));
         };
         FirSet S0, S1, S2;
 #define BCSIM_LOAD(S, I)                                                            \
@@ -116,27 +123,25 @@ __device__ __forceinline__ void fir_mac(const float2* seg, int row, int sub, int
         S.a = r3[I]; S.b = r0[(I) + 1]; S.c = r1[(I) + 1]; S.d = r2[(I) + 1];       \
         S.h0 = tap(4 * (I)); S.h1 = tap(4 * (I) + 1); S.h2 = tap(4 * (I) + 2); S.h3 = tap(4 * (I) + 3); \
     }
-#define BCSIM_MAC(Y, Z, W, SW, H)                                                   \
-    {                                                                               \
-        if (PD) { Y = __ffma2_rn(W, make_float2(H.x, H.y), Y); Z = fmaf(SW, H.z, Z); } \
-        else rmac(Y, W, H);                                                         \
-    }
+#define BCSIM_G(Y, W, H)                                                            \
+    { if (PD) Y = __ffma2_rn(W, make_float2(H.x, H.y), Y); else rmac(Y, W, H); }
+#define BCSIM_H(Y, W, H) { Y = __ffma2_rn(W, make_float2(H.z, H.w), Y); }
 #define BCSIM_ITER(C, P, N, I)                                                      \
     {                                                                               \
         if ((I) + 1 < n4) BCSIM_LOAD(N, (I) + 1)                                    \
-        if (PD) { C.sa = C.a.x + C.a.y; C.sb = C.b.x + C.b.y; C.sc = C.c.x + C.c.y; C.sd = C.d.x + C.d.y; } \
-        BCSIM_MAC(y0, z0, P.b, P.sb, C.h0) BCSIM_MAC(y1, z1, P.c, P.sc, C.h0)       \
-        BCSIM_MAC(y2, z2, P.d, P.sd, C.h0) BCSIM_MAC(y3, z3, C.a, C.sa, C.h0)       \
-        BCSIM_MAC(y0, z0, P.c, P.sc, C.h1) BCSIM_MAC(y1, z1, P.d, P.sd, C.h1)       \
-        BCSIM_MAC(y2, z2, C.a, C.sa, C.h1) BCSIM_MAC(y3, z3, C.b, C.sb, C.h1)       \
-        BCSIM_MAC(y0, z0, P.d, P.sd, C.h2) BCSIM_MAC(y1, z1, C.a, C.sa, C.h2)       \
-        BCSIM_MAC(y2, z2, C.b, C.sb, C.h2) BCSIM_MAC(y3, z3, C.c, C.sc, C.h2)       \
-        BCSIM_MAC(y0, z0, C.a, C.sa, C.h3) BCSIM_MAC(y1, z1, C.b, C.sb, C.h3)       \
-        BCSIM_MAC(y2, z2, C.c, C.sc, C.h3) BCSIM_MAC(y3, z3, C.d, C.sd, C.h3)       \
+        BCSIM_G(G0, P.b, C.h0) BCSIM_G(G1, P.c, C.h0) BCSIM_G(G2, P.d, C.h0) BCSIM_G(G3, C.a, C.h0) \
+        BCSIM_G(G0, P.c, C.h1) BCSIM_G(G1, P.d, C.h1) BCSIM_G(G2, C.a, C.h1) BCSIM_G(G3, C.b, C.h1) \
+        BCSIM_G(G0, P.d, C.h2) BCSIM_G(G1, C.a, C.h2) BCSIM_G(G2, C.b, C.h2) BCSIM_G(G3, C.c, C.h2) \
+        BCSIM_G(G0, C.a, C.h3) BCSIM_G(G1, C.b, C.h3) BCSIM_G(G2, C.c, C.h3) BCSIM_G(G3, C.d, C.h3) \
+        if (PD && (I) >= h_lo && (I) < h_hi) {   /* warp-uniform */                 \
+            BCSIM_H(H0, P.b, C.h0) BCSIM_H(H1, P.c, C.h0) BCSIM_H(H2, P.d, C.h0) BCSIM_H(H3, C.a, C.h0) \
+            BCSIM_H(H0, P.c, C.h1) BCSIM_H(H1, P.d, C.h1) BCSIM_H(H2, C.a, C.h1) BCSIM_H(H3, C.b, C.h1) \
+            BCSIM_H(H0, P.d, C.h2) BCSIM_H(H1, C.a, C.h2) BCSIM_H(H2, C.b, C.h2) BCSIM_H(H3, C.c, C.h2) \
+            BCSIM_H(H0, C.a, C.h3) BCSIM_H(H1, C.b, C.h3) BCSIM_H(H2, C.c, C.h3) BCSIM_H(H3, C.d, C.h3) \
+        }                                                                           \
     }
         // the elements carried into iteration 0: r0[0], r1[0], r2[0]
         S2.b = r0[0]; S2.c = r1[0]; S2.d = r2[0];
-        if (PD) { S2.sb = S2.b.x + S2.b.y; S2.sc = S2.c.x + S2.c.y; S2.sd = S2.d.x + S2.d.y; }
         BCSIM_LOAD(S0, 0)
         for (int i = 0;; i += 3) {
             BCSIM_ITER(S0, S2, S1, i)
@@ -147,14 +152,15 @@ __device__ __forceinline__ void fir_mac(const float2* seg, int row, int sub, int
             if (i + 3 >= n4) break;
         }
 #undef BCSIM_ITER
-#undef BCSIM_MAC
+#undef BCSIM_H
+#undef BCSIM_G
 #undef BCSIM_LOAD
     }
-    if (PD) {   // re = k1 - k3, im = k1 + k2 with k1 = z, (k2, k3) = y
-        out[0] = make_float2(z0 - y0.y, z0 + y0.x); out[1] = make_float2(z1 - y1.y, z1 + y1.x);
-        out[2] = make_float2(z2 - y2.y, z2 + y2.x); out[3] = make_float2(z3 - y3.y, z3 + y3.x);
+    if (PD) {   // y = (H.re - G.im, H.im + G.re)
+        out[0] = make_float2(H0.x - G0.y, H0.y + G0.x); out[1] = make_float2(H1.x - G1.y, H1.y + G1.x);
+        out[2] = make_float2(H2.x - G2.y, H2.y + G2.x); out[3] = make_float2(H3.x - G3.y, H3.y + G3.x);
     } else {
-        out[0] = y0; out[1] = y1; out[2] = y2; out[3] = y3;
+        out[0] = G0; out[1] = G1; out[2] = G2; out[3] = G3;
     }
 }
 
@@ -189,7 +195,7 @@ __global__ void __launch_bounds__(128)
     if (TAPS_SMEM) {
         const int ntaps_pm = __ldg(ph_off + D);
         for (int i = tid; i < ntaps_pm; i += blockDim.x)
-            tp4[i] = PD ? tap_gauss(__ldg(taps_pm + i)) : tap_real(__ldg(taps_pm + i));
+            tp4[i] = PD ? tap_split(__ldg(taps_pm + i)) : tap_real(__ldg(taps_pm + i));
     }
     const long long jbase = (long long)center + (long long)m0 * D - tap_start - (W - 1);
     const long long mmask = (long long)M - 1;
@@ -304,12 +310,32 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
 }
 
 int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph) {
+    // the excitation's support: real parts above 1e-9 of the largest (outside
+    // it the FP64 analytic pulse's real part is rounding residue, set to 0)
+    float re_max = 0.0f;
+    for (int w = 0; w < W; w++) re_max = std::max(re_max, std::fabs(taps[w].x));
+    const float thr = 1e-9f * re_max;
     int n = 0, mx = 0;
     for (int ph = 0; ph < D; ph++) {
         off[ph] = n;
         const int cnt = ph <= W - 1 ? (W - 1 - ph) / D + 1 : 0;
         const int pad = (cnt + 3) / 4 * 4;
-        for (int t = 0; t < pad; t++) out[n + t] = t < cnt ? taps[W - 1 - (ph + t * D)] : make_float2(0.0f, 0.0f);
+        int lo = pad / 4, hi = 0;   // 4-tap iterations holding support taps
+        for (int t = 0; t < pad; t++) {
+            float2 v = make_float2(0.0f, 0.0f);
+            if (t < cnt) {
+                v = taps[W - 1 - (ph + t * D)];
+                if (std::fabs(v.x) <= thr) v.x = 0.0f;
+            }
+            out[n + t] = v;
+            if (v.x != 0.0f) {
+                lo = std::min(lo, t / 4);
+                hi = std::max(hi, t / 4 + 1);
+            }
+        }
+        if (hi <= lo) lo = hi = 0;
+        off[D + 1 + 2 * ph] = lo;
+        off[D + 2 + 2 * ph] = hi;
         n += pad;
         mx = pad > mx ? pad : mx;
     }

@@ -513,7 +513,7 @@ void Simulator::prepare_excitation_tables() {
     BCSIM_CUDA(cudaMemcpyAsync(demod_dev_.get(), dm.data(), dm.size() * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     // the window's taps in the kernel's phase-major order for this decimation
     std::vector<float2> pm((size_t)tap_count_ + 4 * decimation_);
-    std::vector<int> off((size_t)decimation_ + 1);
+    std::vector<int> off((size_t)3 * decimation_ + 1);
     ntaps_pm_ = make_phase_major_taps(fir_taps_host_.data(), (int)tap_count_, decimation_, pm.data(), off.data(),
                                       &max_ph_taps_);
     taps_pm_dev_.reserve(std::max<size_t>(1, (size_t)ntaps_pm_) * sizeof(float2), stream_);

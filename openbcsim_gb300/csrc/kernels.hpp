@@ -165,8 +165,8 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
 // Fused convolution with the analytic pulse (direct FIR over a tap window),
 // IQ demodulation and radial decimation, from fixed-point bins to complex64.
 // taps_pm/ph_off: the window's taps in phase-major order for this decimation
-// (see make_phase_major_taps), ntaps_pm = ph_off[D], max_ph_taps = the longest
-// phase.
+// and the phase table (see make_phase_major_taps), ntaps_pm = ph_off[D],
+// max_ph_taps = the longest phase.
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                        float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
                                        int max_ph_taps, int num_taps, int tap_start, int64_t M, int center,
@@ -174,8 +174,11 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
 
 // Host: the FIR window taps[0..W) rearranged for the convolution kernel:
 // phase ph (0..D-1) holds, for t = 0, 1, ..., the tap w = W - 1 - (ph + t*D),
-// zero-padded to a multiple of 4.  out/off must hold W + 4*D and D + 1 entries.
-// Returns the total count; *max_ph receives the longest padded phase.
+// zero-padded to a multiple of 4; off[0..D] are the phases' offsets and
+// off[D+1+2ph], off[D+2+2ph] the range of 4-tap iterations of phase ph that
+// hold the excitation's support (non-zero real parts; real parts below 1e-9
+// of the largest are set to 0).  out/off must hold W + 4*D and 3*D + 1
+// entries.  Returns the total count; *max_ph receives the longest padded phase.
 int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph);
 
 // Radix sort of (key, value) pairs: key bits [0, end_bit).  temp == nullptr

@@ -49,6 +49,7 @@ constexpr int NA_MAX_DEC = 1024;                                 // radial decim
 constexpr size_t NA_PM_OFF = NA_TAPS_OFF + NA_MAX_TAPS * sizeof(float2);              // phase-major taps
 constexpr size_t NA_PHOFF_OFF = NA_PM_OFF + (NA_MAX_TAPS + 4 * NA_MAX_DEC) * sizeof(float2);  // phase offsets
 constexpr size_t NA_DEMOD_OFF = NA_PHOFF_OFF + 4096 * sizeof(int);
+static_assert(3 * NA_MAX_DEC + 1 <= 4096, "phase table fits its region");
 constexpr int NA_MAX_OUT = 65536;                                // decimated samples per line
 constexpr size_t NA_TOTAL = NA_DEMOD_OFF + NA_MAX_OUT * sizeof(float2);
 constexpr int NA_MAX_FFT = 65536;                                // convolution length M
@@ -67,7 +68,7 @@ std::complex<double> g_fft[NA_MAX_FFT];
 double g_energy[NA_MAX_FFT];
 float2 g_taps[NA_MAX_TAPS];
 float2 g_taps_pm[NA_MAX_TAPS + 4 * NA_MAX_DEC];
-int g_ph_off[NA_MAX_DEC + 1];
+int g_ph_off[3 * NA_MAX_DEC + 1];
 float2 g_demod[NA_MAX_OUT];
 LineGeom g_lines[NA_MAX_LINES];
 int g_ids[NA_MAX_LINES];
@@ -254,7 +255,7 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
     if (e == cudaSuccess) e = cudaMemcpyAsync(ddemod, g_demod, nd * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dpm, g_taps_pm, n_pm * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(dphoff, g_ph_off, (radial_decimation + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(dphoff, g_ph_off, (3 * radial_decimation + 1) * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(bins, 0, (size_t)num_lines * ns * stride * sizeof(unsigned long long), st);
     if (e == cudaSuccess)
