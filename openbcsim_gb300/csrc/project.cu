@@ -766,7 +766,7 @@ constexpr int PAIR_CHUNK = 256;
 // false if the bin is outside [0, ns); otherwise the bin and the sub-sample
 // delay idx - t in samples.
 __device__ __forceinline__ bool pair_bin(df dx, df dy, df dz, float dot, const SimParams& p, int* idx_out,
-                                         float* delay_out, float* r_out) {
+                                         float* delay_out, float* r_out, float* tie_out = nullptr) {
     df r;
     {
         // arc projection: r = +-|d|, |d|^2 = sum hi^2 (exact products) + 2 hi lo
@@ -788,6 +788,8 @@ __device__ __forceinline__ bool pair_bin(df dx, df dy, df dz, float dot, const S
     float rem = t.hi - f;
     if (rem + t.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
     const bool up = (rem - 0.5f) >= -t.lo;
+    // distance (in samples) of t from the rounding boundary
+    if (tie_out) *tie_out = fabsf((rem - 0.5f) + t.lo);
     const float fidx = up ? f + 1.0f : f;
     if (!(fidx >= 0.0f && fidx < (float)p.ns)) return false;
     *idx_out = (int)fidx;
@@ -813,8 +815,14 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                            const LineTile* __restrict__ tiles, const LineBasis* __restrict__ basis,
                            unsigned long long* __restrict__ bins, SimParams p, BeamDev b,
                            const TileBox* __restrict__ boxes, unsigned long long* __restrict__ pair_counts) {
+    // staged scatterers: fixed (x, y, z, a); splines (fp64 mode) the window's
+    // control points relative to its first one (R, in sr), the global index for
+    // the exact re-evaluation at rounding ties; splines (reference mode) the
+    // control points themselves
     __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? MAX_SPLINE_DEGREE + 1 : 1)];
     __shared__ float sa[PAIR_CHUNK];
+    __shared__ float4 sr[SPLINE && !REF ? PAIR_CHUNK : 1];
+    __shared__ int sidx[SPLINE && !REF ? PAIR_CHUNK : 1];
     __shared__ int s_kept;   // scatterers of the chunk kept for the tile
     const LineTile tile = tiles[blockIdx.y];
     int64_t count = n, list_off = 0;
@@ -931,7 +939,17 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         if (ok) {
             const int d = base + __popc(bal & ((1u << lane) - 1u));
             if (SPLINE) {
-                for (int k = 0; k < span; k++) sp[d * span + k] = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+                if (REF) {
+                    for (int k = 0; k < span; k++) sp[d * span + k] = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+                } else {
+                    const float4 R = __ldg(cps + (int64_t)(tile.mu - degree) * n + s);
+                    for (int k = 0; k < span; k++) {
+                        const float4 c = __ldg(cps + (int64_t)(tile.mu - degree + k) * n + s);
+                        sp[d * span + k] = make_float4(c.x - R.x, c.y - R.y, c.z - R.z, 0.0f);
+                    }
+                    sr[d] = R;
+                    sidx[d] = (int)s;
+                }
             } else {
                 sp[d] = make_float4(lo_x, lo_y, lo_z, a);
             }
@@ -951,16 +969,19 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         if (!REF) {
             // FP32 position relative to the origin
             float fx, fy, fz;
+            float Sx = 0.f, Sy = 0.f, Sz = 0.f;   // sum_k B_k (C_k - R)
+            float4 R = make_float4(0.f, 0.f, 0.f, 0.f);
             if (SPLINE) {
-                fx = 0.f; fy = 0.f; fz = 0.f;
+                // the basis sums to one: P = R + sum_k B_k (C_k - R)
+                R = sr[i];
 #pragma unroll
                 for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
                     if (k < np) {
                         const float4 c = sp[i * span + win + k];
-                        fx = fmaf(bh[k], c.x, fx); fy = fmaf(bh[k], c.y, fy); fz = fmaf(bh[k], c.z, fz);
+                        Sx = fmaf(bh[k], c.x, Sx); Sy = fmaf(bh[k], c.y, Sy); Sz = fmaf(bh[k], c.z, Sz);
                     }
                 }
-                fx -= ox; fy -= oy; fz -= oz;
+                fx = (R.x - ox) + Sx; fy = (R.y - oy) + Sy; fz = (R.z - oz) + Sz;
             } else {
                 const float4 c = sp[i];
                 fx = c.x - ox; fy = c.y - oy; fz = c.z - oz;
@@ -978,15 +999,35 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                 if (!(tl > -1.001f && tl < (float)(b.nl - 1) + 0.001f && te > -1.001f && te < (float)(b.ne - 1) + 0.001f))
                     continue;
             }
-            // exact position relative to the origin as float pairs
+            // position relative to the origin as float pairs: R - o exactly, plus
+            // the FP32 sum S (its error, ~1e-8 of the control points' spread, is
+            // ~2e-5 of a sample; bins within 1e-3 of a sample of a rounding tie
+            // are decided again from the exact float-pair spline sum below)
             df dx, dy, dz;
             if (SPLINE) {
+                auto near = [](float r, float o, float sum) {
+                    const df a = two_sum(r, -o);
+                    const df b = two_sum(a.hi, sum);
+                    return fast_two_sum(b.hi, b.lo + a.lo);
+                };
+                dx = near(R.x, ox, Sx);
+                dy = near(R.y, oy, Sy);
+                dz = near(R.z, oz, Sz);
+            } else {
+                const float4 c = sp[i];
+                dx = two_sum(c.x, -ox);
+                dy = two_sum(c.y, -oy);
+                dz = two_sum(c.z, -oz);
+            }
+            // the exact float-pair sum sum_k (bh_k + bl_k) C_k - o, control points from global memory
+            auto exact_position = [&]() {
                 df sx = df_make(0.f, 0.f), sy = df_make(0.f, 0.f), sz = df_make(0.f, 0.f);
                 float ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;   // accumulated low parts
+                const int gs = sidx[i];
 #pragma unroll
                 for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
                     if (k < np) {
-                        const float4 c = sp[i * span + win + k];
+                        const float4 c = __ldg(cps + (int64_t)(tile.mu - degree + win + k) * n + gs);
                         const df px = two_prod(bh[k], c.x), py = two_prod(bh[k], c.y), pz = two_prod(bh[k], c.z);
                         const df tx = two_sum(sx.hi, px.hi), ty = two_sum(sy.hi, py.hi), tz = two_sum(sz.hi, pz.hi);
                         sx.hi = tx.hi; sy.hi = ty.hi; sz.hi = tz.hi;
@@ -999,30 +1040,48 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                 dx = fast_two_sum(ux.hi, ux.lo + ex_);
                 dy = fast_two_sum(uy.hi, uy.lo + ey_);
                 dz = fast_two_sum(uz.hi, uz.lo + ez_);
-            } else {
-                const float4 c = sp[i];
-                dx = two_sum(c.x, -ox);
-                dy = two_sum(c.y, -oy);
-                dz = two_sum(c.z, -oz);
-            }
+            };
             const float fdx = dx.hi + dx.lo, fdy = dy.hi + dy.lo, fdz = dz.hi + dz.lo;
             const float dot = fmaf(fdz, rz, fmaf(fdy, ry, fdx * rx));
             float delay, rr;
             if (p.arc) {
-                if (!pair_bin(dx, dy, dz, dot, p, &idx, &delay, &rr)) continue;
+                if (SPLINE) {
+                    float tie = 1.0f;
+                    const bool in = pair_bin(dx, dy, dz, dot, p, &idx, &delay, &rr, &tie);
+                    if (tie < 1e-3f) {   // near a rounding tie: decide from the exact sum
+                        exact_position();
+                        const float xd = dx.hi + dx.lo, yd = dy.hi + dy.lo, zd = dz.hi + dz.lo;
+                        if (!pair_bin(dx, dy, dz, fmaf(zd, rz, fmaf(yd, ry, xd * rx)), p, &idx, &delay, &rr)) continue;
+                    } else if (!in) {
+                        continue;
+                    }
+                } else {
+                    if (!pair_bin(dx, dy, dz, dot, p, &idx, &delay, &rr)) continue;
+                }
             } else {
                 // radial coordinate = projection on the line direction
-                const df r = df_add(df_add(df_mul_f(dx, rx), df_mul_f(dy, ry)), df_mul_f(dz, rz));
-                rr = r.hi + r.lo;
-                const df t = df_mul(r, df_make(p.k_hi, p.k_lo));
-                float f = floorf(t.hi);
-                float rem = t.hi - f;
-                if (rem + t.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
-                const bool up = (rem - 0.5f) >= -t.lo;
-                const float fidx = up ? f + 1.0f : f;
-                if (!(fidx >= 0.0f && fidx < (float)p.ns)) continue;
-                idx = (int)fidx;
-                delay = (up ? 1.0f : 0.0f) - rem - t.lo;
+                auto linear_bin = [&](float* tie) {
+                    const df r = df_add(df_add(df_mul_f(dx, rx), df_mul_f(dy, ry)), df_mul_f(dz, rz));
+                    rr = r.hi + r.lo;
+                    const df t = df_mul(r, df_make(p.k_hi, p.k_lo));
+                    float f = floorf(t.hi);
+                    float rem = t.hi - f;
+                    if (rem + t.lo < 0.0f) { f -= 1.0f; rem += 1.0f; }
+                    const bool up = (rem - 0.5f) >= -t.lo;
+                    *tie = fabsf((rem - 0.5f) + t.lo);
+                    const float fidx = up ? f + 1.0f : f;
+                    if (!(fidx >= 0.0f && fidx < (float)p.ns)) return false;
+                    idx = (int)fidx;
+                    delay = (up ? 1.0f : 0.0f) - rem - t.lo;
+                    return true;
+                };
+                float tie = 1.0f;
+                bool in = linear_bin(&tie);
+                if (SPLINE && tie < 1e-3f) {   // near a rounding tie: decide from the exact sum
+                    exact_position();
+                    in = linear_bin(&tie);
+                }
+                if (!in) continue;
             }
             if (BEAM == BEAM_LUT) {
                 const float tr = (rr - b.rf) * b.inv_dr;
