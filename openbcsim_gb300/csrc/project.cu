@@ -481,6 +481,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     // record carries its plane's offset in shared memory (in B.z).
     __shared__ int s_r0_min, s_r0_max;
     bool all_staged = false;
+    // 0x4B000000 = bits(2^23): the table indices' float bit patterns carry it
+    const unsigned lut_addr0 = (unsigned)__cvta_generic_to_shared(smL) - 0x4B000000u * 16u * (unsigned)(lut_row + 1);
     if (BEAM == BEAM_LUT && !REF && lut_staged > 0) {
         if (tid == 0) {
             s_r0_min = 0x7fffffff;
@@ -503,7 +505,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         all_staged = s_r0_min >= lut_base && s_r0_max < lut_base + lut_staged;
         if (all_staged) {
             for (int r = tid; r < cnt; r += blockDim.x)
-                smB[r].z = __int_as_float((__float_as_int(smB[r].z) - lut_base) * lut_splane);
+                // the shared byte address of the record's plane, less the table
+                // index bias: corner (l0, e0) of a pair then lies at
+                // B.z + bits(l0 + 2^23) * 16 lut_row + bits(e0 + 2^23) * 16 (mod 2^32)
+                smB[r].z = __uint_as_float(lut_addr0 + (unsigned)((__float_as_int(smB[r].z) - lut_base) * lut_splane) * 16u);
             __syncthreads();
         }
     }
@@ -697,10 +702,14 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                                 const float fl = fle.x, fe = fle.y;
                                 const int r0 = __float_as_int(B.z);
                                 float4 P, Q;
-                                if (STAGED) {   // B.z holds the record's plane offset in shared memory
-                                    const float4* pl = smL + r0 + l0 * lut_row + e0;
-                                    P = pl[0];
-                                    Q = pl[lut_row];
+                                if (STAGED) {   // B.z: the record's plane address, see above
+                                    const unsigned a = __float_as_uint(B.z) +
+                                                       __float_as_uint(t2.x) * (16u * (unsigned)lut_row) +
+                                                       __float_as_uint(t2.y) * 16u;
+                                    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                        : "=f"(P.x), "=f"(P.y), "=f"(P.z), "=f"(P.w) : "r"(a));
+                                    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                                        : "=f"(Q.x), "=f"(Q.y), "=f"(Q.z), "=f"(Q.w) : "r"(a + 16u * (unsigned)lut_row));
                                 } else if ((unsigned)(r0 - lut_base) < (unsigned)lut_staged) {   // warp-uniform
                                     const float4* pl = smL + (r0 - lut_base) * lut_splane + l0 * lut_row + e0;
                                     P = pl[0];
