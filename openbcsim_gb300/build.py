@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 
-CU_SOURCES = ["project.cu", "conv.cu", "noalloc.cu", "ingest.cu", "imaging.cu"]
+CU_SOURCES = ["project.cu", "conv.cu", "fftconv.cu", "noalloc.cu", "ingest.cu", "imaging.cu"]
 CPP_SOURCES = ["engine.cpp", "host_dsp.cpp", "capi.cpp", "batch.cpp", "server.cpp", "imaging_host.cpp"]
 HEADERS = ["kernels.hpp", "dfloat.cuh", "fixedpoint.cuh", "async_copy.cuh", "engine.hpp", "host_dsp.hpp", "imaging.hpp", "imaging_host.hpp"]
 

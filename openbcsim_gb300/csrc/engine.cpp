@@ -198,6 +198,14 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
         if (!(v >= 0.0 && v < 1.0)) throw SimError(BCSIM_E_INVALID, "fir_tail_energy must be in [0, 1)");
         if (v != fir_tail_) tables_valid_ = false;
         fir_tail_ = v;
+    } else if (key == "convolution") {
+        int v;
+        if (value == "auto") v = 0;
+        else if (value == "fir") v = 1;
+        else if (value == "fft") v = 2;
+        else throw SimError(BCSIM_E_INVALID, "invalid value for convolution (auto | fir | fft)");
+        if (v != convolution_) tables_valid_ = false;
+        convolution_ = v;
     } else if (key == "wide_cta") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         wide_cta_ = b;
@@ -248,6 +256,9 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "store_kernel_details") return store_details_ ? "on" : "off";
     if (key == "precision_mode") return mode_ == MODE_FP64 ? "fp64" : "reference";
     if (key == "fir_tail_energy") return fmt_double(fir_tail_);
+    if (key == "convolution") return convolution_ == 0 ? "auto" : convolution_ == 1 ? "fir" : "fft";
+    // the route the last prepared configuration took ("" before the first simulation)
+    if (key == "convolution_route") return tables_valid_ ? (use_fft_ ? "fft" : "fir") : "";
     if (key == "tile_lines") return std::to_string(tile_lines_);
     if (key == "cull") return cull_ ? "on" : "off";
     if (key == "record_cache") return record_cache_ ? "on" : "off";
@@ -484,6 +495,18 @@ std::vector<double> Simulator::get_debug_data(const std::string& key) const {
 // ---------------------------------------------------------------------------
 // derived tables
 // ---------------------------------------------------------------------------
+
+// Automatic convolution route: the direct FIR evaluates nd outputs of `window`
+// complex MACs per line, the FFT route two transforms of M points (the inverse
+// shortened by the decimation fold); the FIR wins for short windows.
+// Measured on GB300: the FIR costs ~0.23 ns per line per output-tap, the FFT
+// route ~1.3 ns per line per M log2 M.
+static bool fft_preferred(int64_t M, int64_t nd, int64_t window) {
+    int lg = 0;
+    while ((int64_t(1) << lg) < M) lg++;
+    return (double)nd * (double)window > 6.0 * (double)M * (double)lg;
+}
+
 void Simulator::prepare_excitation_tables() {
     if (tables_valid_) return;
     const int64_t ntaps = (int64_t)taps_.size();
@@ -494,7 +517,10 @@ void Simulator::prepare_excitation_tables() {
     // the FIR window depends on the excitation, M and the tail energy only:
     // recompute it (an M-point FFT in double) only when one of them changed
     if (!(fir_key_taps_ == taps_ && fir_key_M_ == M_ && fir_key_tail_ == fir_tail_)) {
-        const auto ha = analytic_pulse(taps_, M_);
+        analytic_spec_ = analytic_spectrum(taps_, M_);
+        std::vector<std::complex<double>> ha = analytic_spec_;
+        fft_double(ha, +1);
+        for (auto& v : ha) v /= (double)M_;
         choose_tap_window(ha, (int)ntaps, fir_tail_, &tap_start_, &tap_count_);
         std::vector<float2> taps((size_t)tap_count_);
         for (int64_t w = 0; w < tap_count_; w++) {
@@ -520,6 +546,28 @@ void Simulator::prepare_excitation_tables() {
     ph_off_dev_.reserve(off.size() * sizeof(int), stream_);
     BCSIM_CUDA(cudaMemcpyAsync(taps_pm_dev_.get(), pm.data(), (size_t)ntaps_pm_ * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaMemcpyAsync(ph_off_dev_.get(), off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
+    // convolution route: the FFT when its line fits one CTA's shared memory and
+    // it costs less than the direct FIR's nd * window complex MACs per line
+    int smem_optin = 0;
+    BCSIM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+    const bool fft_ok = fft_convolution_supported(M_) && ns_ <= M_ &&
+                        fft_convolution_smem(M_, decimation_) <= (size_t)smem_optin;
+    if (convolution_ == 2 && !fft_ok)
+        throw SimError(BCSIM_E_INVALID, "convolution=fft needs a power-of-two convolution length M in [256, 16384] "
+                                        "(this configuration has M = " + std::to_string(M_) + ")");
+    use_fft_ = convolution_ == 2 || (convolution_ == 0 && fft_ok && fft_preferred(M_, nd_, tap_count_));
+    std::vector<float2> hold_spec, hold_tw;
+    if (use_fft_) {
+        hold_spec.resize((size_t)M_);
+        hold_tw.resize((size_t)M_);
+        make_fft_tables(analytic_spec_.data(), M_, center_, decimation_, hold_spec.data(), hold_tw.data());
+        fft_spec_dev_.reserve((size_t)M_ * sizeof(float2), stream_);
+        fft_tw_dev_.reserve((size_t)M_ * sizeof(float2), stream_);
+        BCSIM_CUDA(cudaMemcpyAsync(fft_spec_dev_.get(), hold_spec.data(), (size_t)M_ * sizeof(float2),
+                                   cudaMemcpyHostToDevice, stream_));
+        BCSIM_CUDA(cudaMemcpyAsync(fft_tw_dev_.get(), hold_tw.data(), (size_t)M_ * sizeof(float2),
+                                   cudaMemcpyHostToDevice, stream_));
+    }
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
     tables_valid_ = true;
 }
@@ -1230,11 +1278,18 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         const int l0 = (int)((int64_t)L * k / nblocks), l1 = (int)((int64_t)L * (k + 1) / nblocks);
         if (l1 <= l0) continue;
         ++launches;
-        BCSIM_CUDA(launch_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns, p.phase_delay,
-                                              std::ldexp(1.0f, -p.log2scale), taps_pm_dev_.as<float2>(),
-                                              ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_, (int)tap_count_,
-                                              (int)tap_start_, M_, center_, decimation_, (int)nd_,
-                                              demod_dev_.as<float2>(), dev_out + (int64_t)l0 * nd_, st));
+        if (use_fft_)
+            BCSIM_CUDA(launch_fft_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns,
+                                                      p.phase_delay, std::ldexp(1.0f, -p.log2scale),
+                                                      fft_spec_dev_.as<float2>(), fft_tw_dev_.as<float2>(), M_,
+                                                      decimation_, (int)nd_, demod_dev_.as<float2>(),
+                                                      dev_out + (int64_t)l0 * nd_, st));
+        else
+            BCSIM_CUDA(launch_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns, p.phase_delay,
+                                                  std::ldexp(1.0f, -p.log2scale), taps_pm_dev_.as<float2>(),
+                                                  ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_, (int)tap_count_,
+                                                  (int)tap_start_, M_, center_, decimation_, (int)nd_,
+                                                  demod_dev_.as<float2>(), dev_out + (int64_t)l0 * nd_, st));
         if (host_out) {
             const cudaStream_t cs = copy_stream_.s;
             BCSIM_CUDA(cudaEventRecord(ev_blocks_[k], st));

@@ -225,6 +225,7 @@ private:
     bool store_details_ = false;
     int mode_ = MODE_FP64;
     double fir_tail_ = 1e-10;
+    int convolution_ = 0;   // 0 = automatic, 1 = direct FIR, 2 = FFT
     int tile_lines_ = 0;   // 0 = automatic
     bool cull_ = true;     // exact culling of zero-weight (scatterer, line-slot) pairs
     bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
@@ -283,6 +284,9 @@ private:
     double fir_key_tail_ = -1.0;
     DeviceBuffer demod_dev_, taps_pm_dev_, ph_off_dev_;
     std::vector<float2> fir_taps_host_;   // the FIR window taps, in window order
+    std::vector<std::complex<double>> analytic_spec_;   // FFT_M(h) * hilbert mask, for the FFT route
+    bool use_fft_ = false;   // convolution by FFT (fftconv.cu) rather than the direct FIR
+    DeviceBuffer fft_spec_dev_, fft_tw_dev_;
     int ntaps_pm_ = 0, max_ph_taps_ = 0;
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;

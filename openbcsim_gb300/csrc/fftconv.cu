@@ -1,0 +1,377 @@
+// fftconv.cu -- pulse convolution, IQ demodulation and radial decimation by
+// FFT, for long analytic pulses.
+//
+// The reference's convolution is a length-M circular convolution with the
+// analytic pulse, by FFT, multiply and inverse FFT (src/core/BeamConvolver.cpp:
+// 64-91; GPU: cuFFT + MultiplyFftKernel, GpuAlgorithm.cpp:280-325), followed by
+// the demodulation of every sample and the decimation (CpuAlgorithm.cpp:353-365):
+//     out[m] = y[center + m D] * exp(-j 2 pi fd/fs m D),
+//     y = IFFT_M(FFT_M(bins) * H),  H = FFT_M(h) * hilbert_mask.
+// The direct FIR (conv.cu) costs one complex MAC per tap and output, which for
+// long pulses (the Hilbert part of h_a decays slowly: windows of ~2000 taps)
+// exceeds the FFT's O(log M) per sample.  This kernel runs the FFT route for
+// one line per CTA, entirely in shared memory (M <= 16384):
+//
+//   1. forward transform, decimation in frequency, in place: radix-R passes
+//      (R = 16, the second pass 2, 4 or 8 to make up log2 M); a pass treats
+//      the array as blocks of length L, and for each offset n1 < L/R transforms
+//      the R elements n1 + j L/R in registers and multiplies output q by the
+//      twiddle W_L^(n1 q).  The first pass reads the fixed-point bins straight
+//      from global memory, sixteen independent loads per thread.  The spectrum
+//      ends in digit-reversed order, which the host's copy of H matches (so no
+//      reordering pass is needed);
+//   2. the last forward pass, the multiply by H (pre-scaled by 1/M and by the
+//      phase ramp exp(+j 2 pi center k / M), so that the result starts at
+//      sample `center`), the decimation fold and the first inverse pass run in
+//      registers: with F the largest power of two dividing D (F <= 16), the
+//      samples y[F n'] are the length-M/F inverse transform of the spectrum
+//      folded onto k mod M/F, and the F terms of a fold lie in one thread's
+//      block of 16;
+//   3. inverse transform of length M/F, decimation in time: the exact inverse
+//      passes in reverse order, the last one writing out[m] = y[F n'] times
+//      the demodulation factor for the n' = m D / F.
+//
+// Shared memory holds the array padded by one float2 per 16 (element i at
+// i + i/16): every pass then reads and writes without bank conflicts (two
+// wavefronts per warp access of 8 bytes).  Twiddles W_M^e, e < M, come from a
+// host-made table (double precision rounded once), through the L1 cache.
+// FP32 throughout: the relative RMS error is ~2e-7 of the IQ.
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <type_traits>
+#include <vector>
+#include "fixedpoint.cuh"
+#include "kernels.hpp"
+
+namespace bcsim_gb300 {
+
+namespace {
+
+constexpr int FFT_THREADS = 512;
+
+// cos(2 pi k / 16) and sin(2 pi k / 16) for 0 <= k < 8
+__host__ __device__ constexpr float cos16(int k) {
+    return k == 0   ? 1.0f
+           : k == 1 ? 0.92387953251128674f
+           : k == 2 ? 0.70710678118654752f
+           : k == 3 ? 0.38268343236508977f
+           : k == 4 ? 0.0f
+           : k == 5 ? -0.38268343236508977f
+           : k == 6 ? -0.70710678118654752f
+                    : -0.92387953251128674f;
+}
+__host__ __device__ constexpr float sin16(int k) { return cos16(4 - k < 0 ? k - 4 : 4 - k); }
+
+__host__ __device__ constexpr int bit_reverse(int q, int R) {
+    int r = 0;
+    for (int b = 1; b < R; b <<= 1) r = (r << 1) | ((q & b) ? 1 : 0);
+    return r;
+}
+
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 w) {
+    return make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+__device__ __forceinline__ float2 cmul_conj(float2 a, float2 w) {   // a * conj(w)
+    return make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+// a * W_16^e (forward: W = exp(-j 2 pi / 16); inverse: its conjugate), 0 <= e < 8
+template <bool INV>
+__device__ __forceinline__ float2 mul_w16(float2 a, int e) {
+    if (e == 0) return a;
+    if (e == 4) return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+    const float c = cos16(e), s = INV ? sin16(e) : -sin16(e);
+    return make_float2(a.x * c - a.y * s, a.x * s + a.y * c);
+}
+
+// In-register DFT of R <= 16 points (natural order in), radix-2 decimation in
+// frequency: output q lands in v[bit_reverse(q, R)].
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 (&v)[R]) {
+#pragma unroll
+    for (int half = R / 2; half >= 1; half >>= 1) {
+#pragma unroll
+        for (int b = 0; b < R; b += 2 * half) {
+#pragma unroll
+            for (int j = 0; j < half; j++) {
+                const float2 a = v[b + j], c = v[b + j + half];
+                v[b + j] = cadd(a, c);
+                v[b + j + half] = mul_w16<INV>(csub(a, c), j * (16 / (2 * half)));
+            }
+        }
+    }
+}
+
+// Twiddles W^(e q), q < R, of one task: the powers of two W^e, W^2e, W^4e,
+// W^8e from the table (tw[x] = W^x), the others as products of those (at most
+// three roundings deep: ~2e-7 relative).
+template <int R>
+__device__ __forceinline__ void task_twiddles(const float2* __restrict__ tw, int e, float2 (&w)[R]) {
+    w[0] = make_float2(1.0f, 0.0f);
+#pragma unroll
+    for (int q = 1; q < R; q <<= 1) w[q] = __ldg(tw + e * q);
+#pragma unroll
+    for (int q = 3; q < R; q++)
+        if (q & (q - 1)) w[q] = cmul(w[q & -q], w[q - (q & -q)]);
+}
+
+// One in-place pass of radix R over an array of Mc elements in blocks of
+// length L: forward (output q of offset n1 times W_L^(n1 q)) or its exact
+// inverse (input q times conj W_L^(n1 q), inverse DFT).  tw[e] = W_M^e; the
+// twiddle W_L^x is tw[x * ts], ts = M / L.  A thread takes 16 / R tasks at a
+// time, so that every pass keeps sixteen loads in flight per thread.
+template <int R, bool INV>
+__device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const float2* __restrict__ tw) {
+    constexpr int G = 16 / R;
+    const int S = L / R;
+    const int T = Mc / R;
+    for (int t0 = threadIdx.x; t0 < T; t0 += blockDim.x * G) {
+        float2 v[G][R], w[G][R];
+        int base[G];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const int t = min(t0 + g * (int)blockDim.x, T - 1);   // (a clamped task is recomputed, not stored)
+            const int n1 = t & (S - 1);
+            base[g] = (t - n1) * R + n1;
+            task_twiddles<R>(tw, n1 * ts, w[g]);
+#pragma unroll
+            for (int j = 0; j < R; j++) v[g][j] = s[fpad(base[g] + j * S)];
+        }
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (INV) {
+#pragma unroll
+                for (int q = 1; q < R; q++) v[g][q] = cmul_conj(v[g][q], w[g][q]);
+            }
+            dft<R, INV>(v[g]);
+        }
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (t0 + g * (int)blockDim.x >= T) continue;
+#pragma unroll
+            for (int q = 0; q < R; q++) {
+                float2 y = v[g][bit_reverse(q, R)];
+                if (!INV && q > 0) y = cmul(y, w[g][q]);
+                s[fpad(base[g] + q * S)] = y;
+            }
+        }
+    }
+}
+
+// The fused middle: last forward pass (blocks of 16, no twiddles), multiply by
+// the spectrum, fold by F = 16 / RF, first inverse pass (radix RF, blocks of
+// RF, no twiddles), into dst (dst == s when RF == 16: same positions).
+template <int RF>
+__device__ __forceinline__ void fft_middle(const float2* s, float2* dst, int M, const float4* __restrict__ spec4) {
+    for (int b = threadIdx.x; b < M / 16; b += blockDim.x) {
+        float2 v[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] = s[fpad(b * 16 + j)];
+        dft<16, false>(v);
+        float2 f[RF];
+#pragma unroll
+        for (int r = 0; r < RF; r++) f[r] = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int q = 0; q < 16; q += 2) {
+            const float4 h = __ldg(spec4 + b * 8 + q / 2);   // spectrum entries q, q + 1
+            f[q % RF] = cadd(f[q % RF], cmul(v[bit_reverse(q, 16)], make_float2(h.x, h.y)));
+            f[(q + 1) % RF] = cadd(f[(q + 1) % RF], cmul(v[bit_reverse(q + 1, 16)], make_float2(h.z, h.w)));
+        }
+        if (RF > 1) dft<RF, true>(f);
+#pragma unroll
+        for (int k = 0; k < RF; k++) dst[fpad(b * RF + k)] = f[bit_reverse(k, RF)];
+    }
+}
+
+template <bool PD>
+__device__ __forceinline__ float2 load_bin(const long long* __restrict__ lb, int n, int ns, float inv_scale) {
+    if (n >= ns) return make_float2(0.0f, 0.0f);
+    if (PD) {
+        const longlong2 v = __ldg(reinterpret_cast<const longlong2*>(lb) + n);
+        return make_float2(fix2f(v.x, inv_scale), fix2f(v.y, inv_scale));
+    }
+    return make_float2(fix2f(__ldg(lb + n), inv_scale), 0.0f);
+}
+
+// One line per CTA.  Passes: forward radix 16 at L = M (from the bins), radix
+// RS (1 = none) at L = M/16, radix 16 down to L = 256, the middle at L = 16;
+// inverse (length M' = M/F) radix 16 from L' = 16 (16/F) up to M'/(16 RS),
+// radix RS at L' = M'/16, the output pass radix 16 at L' = M'.  MINB: CTAs per
+// SM the register allocation leaves room for.
+template <int RS, bool PD, int MINB>
+__global__ void __launch_bounds__(FFT_THREADS, MINB)
+    fft_convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale, int M,
+                                   int F, const float4* __restrict__ spec4, const float2* __restrict__ tw, int D,
+                                   int nd, const float2* __restrict__ demod, float2* __restrict__ out) {
+    extern __shared__ __align__(16) float2 fsm[];
+    float2* s = fsm;
+    const int Mp = M / F;
+    float2* s2 = F > 1 ? fsm + fpad(M) : fsm;
+    const int line = blockIdx.x;
+    const long long* lb = reinterpret_cast<const long long*>(bins) + (int64_t)line * ns * (PD ? 2 : 1);
+
+    // forward pass 0 (radix 16, L = M), from the bins: sixteen independent
+    // loads per task
+    {
+        const int S = M / 16;
+        for (int t = threadIdx.x; t < S; t += blockDim.x) {
+            float2 v[16], w[16];
+            task_twiddles<16>(tw, t, w);
+#pragma unroll
+            for (int j = 0; j < 16; j++) v[j] = load_bin<PD>(lb, t + j * S, ns, inv_scale);
+            dft<16, false>(v);
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                float2 y = v[bit_reverse(q, 16)];
+                if (q > 0) y = cmul(y, w[q]);
+                s[fpad(t + q * S)] = y;
+            }
+        }
+    }
+    __syncthreads();
+    int L = M / 16;
+    if (RS > 1) {
+        fft_pass<RS, false>(s, M, L, M / L, tw);
+        __syncthreads();
+        L /= RS;
+    }
+    for (; L > 16; L /= 16) {
+        fft_pass<16, false>(s, M, L, M / L, tw);
+        __syncthreads();
+    }
+    switch (F) {
+        case 1: fft_middle<16>(s, s2, M, spec4); break;
+        case 2: fft_middle<8>(s, s2, M, spec4); break;
+        case 4: fft_middle<4>(s, s2, M, spec4); break;
+        case 8: fft_middle<2>(s, s2, M, spec4); break;
+        default: fft_middle<1>(s, s2, M, spec4); break;
+    }
+    __syncthreads();
+    for (L = (16 / F) * 16; L <= Mp / (16 * RS); L *= 16) {
+        fft_pass<16, true>(s2, Mp, L, M / L, tw);
+        __syncthreads();
+    }
+    if (RS > 1) {
+        fft_pass<RS, true>(s2, Mp, Mp / 16, M / (Mp / 16), tw);
+        __syncthreads();
+    }
+    // output pass (radix 16, L' = M'): samples y[F n'], n' = k1 + k2 M'/16;
+    // output m takes n' = m D / F
+    {
+        const int S = Mp / 16;
+        const int DF = D / F;
+        for (int k1 = threadIdx.x; k1 < S; k1 += blockDim.x) {
+            float2 v[16], w[16];
+            task_twiddles<16>(tw, k1 * F, w);
+#pragma unroll
+            for (int q = 0; q < 16; q++) v[q] = s2[fpad(k1 + q * S)];
+#pragma unroll
+            for (int q = 1; q < 16; q++) v[q] = cmul_conj(v[q], w[q]);
+            dft<16, true>(v);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                const int n = k1 + k * S;
+                const int m = n / DF;
+                if (m * DF == n && m < nd) out[(int64_t)line * nd + m] = cmul(v[bit_reverse(k, 16)], __ldg(demod + m));
+            }
+        }
+    }
+}
+
+// the radix between the first pass and the radix-16 passes: M = 16 RS 16^k
+int fft_mid_radix(int64_t M) {
+    int n = 0;
+    while ((int64_t(1) << n) < M) n++;
+    return n % 4 ? 1 << (n % 4) : 1;
+}
+
+}  // namespace
+
+bool fft_convolution_supported(int64_t M) { return M >= 256 && M <= FFT_MAX_M && (M & (M - 1)) == 0; }
+
+int fft_fold(int D) {
+    int F = 1;
+    while (F < 16 && D % (2 * F) == 0) F *= 2;
+    return F;
+}
+
+size_t fft_convolution_smem(int64_t M, int D) {
+    const int64_t F = fft_fold(D);
+    const int64_t words = (M + M / 16) + (F > 1 ? (M / F + M / F / 16) : 0);
+    return (size_t)words * sizeof(float2);
+}
+
+void make_fft_tables(const std::complex<double>* H, int64_t M, int center, int D, float2* spec, float2* tw) {
+    // position p of the forward transform's output holds frequency
+    // k = q_0 + R_0 (q_1 + R_1 (q_2 + ...)), p = q_0 M/R_0 + q_1 M/(R_0 R_1) + ...
+    std::vector<int> radices{16};
+    if (fft_mid_radix(M) > 1) radices.push_back(fft_mid_radix(M));
+    int64_t rest = M / 16 / fft_mid_radix(M);
+    for (; rest > 1; rest /= 16) radices.push_back(16);
+    const double two_pi = 6.283185307179586;
+    for (int64_t p = 0; p < M; p++) {
+        int64_t rem = p, Lc = M, mult = 1, k = 0;
+        for (int R : radices) {
+            Lc /= R;
+            const int64_t q = rem / Lc;
+            rem -= q * Lc;
+            k += mult * q;
+            mult *= R;
+        }
+        // H(k) exp(+j 2 pi center k / M) / M: the inverse transform then starts at `center`
+        const double ph = two_pi * (double)((int64_t)center * k % M) / (double)M;
+        const std::complex<double> v = H[k] * std::complex<double>(std::cos(ph), std::sin(ph)) / (double)M;
+        spec[p] = make_float2((float)v.real(), (float)v.imag());
+    }
+    for (int64_t e = 0; e < M; e++) {
+        const double ph = -two_pi * (double)e / (double)M;
+        tw[e] = make_float2((float)std::cos(ph), (float)std::sin(ph));
+    }
+    (void)D;
+}
+
+cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
+                                           float inv_scale, const float2* spec, const float2* tw, int64_t M,
+                                           int decimation, int nd, const float2* demod, float2* out,
+                                           cudaStream_t stream) {
+    if (num_lines <= 0 || nd <= 0) return cudaSuccess;
+    if (!fft_convolution_supported(M) || ns > M) return cudaErrorInvalidValue;
+    const int F = fft_fold(decimation);
+    const size_t smem = fft_convolution_smem(M, decimation);
+    const int RS = fft_mid_radix(M);
+    const bool two = 2 * smem <= 227 * 1024;   // two CTAs per SM fit: leave them the registers
+    auto launch = [&](auto k) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<num_lines, FFT_THREADS, smem, stream>>>(bins, ns, inv_scale, (int)M, F,
+                                                   reinterpret_cast<const float4*>(spec), tw, decimation, nd, demod,
+                                                   out);
+        return cudaGetLastError();
+    };
+    auto pick = [&](auto pd) -> cudaError_t {
+        constexpr bool PD = decltype(pd)::value;
+        if (two) {
+            switch (RS) {
+                case 2: return launch(fft_convolve_demodulate_kernel<2, PD, 2>);
+                case 4: return launch(fft_convolve_demodulate_kernel<4, PD, 2>);
+                case 8: return launch(fft_convolve_demodulate_kernel<8, PD, 2>);
+                default: return launch(fft_convolve_demodulate_kernel<1, PD, 2>);
+            }
+        }
+        switch (RS) {
+            case 2: return launch(fft_convolve_demodulate_kernel<2, PD, 1>);
+            case 4: return launch(fft_convolve_demodulate_kernel<4, PD, 1>);
+            case 8: return launch(fft_convolve_demodulate_kernel<8, PD, 1>);
+            default: return launch(fft_convolve_demodulate_kernel<1, PD, 1>);
+        }
+    };
+    return phase_delay ? pick(std::true_type{}) : pick(std::false_type{});
+}
+
+}  // namespace bcsim_gb300

@@ -89,4 +89,19 @@ BCSIM_HD float ll2f_rn(long long v) {
     return fp_from_bits(bits | (v < 0 ? 0x80000000u : 0u));
 }
 
+#if defined(__CUDACC__)
+// Fixed-point bin -> float (times inv_scale = 2^-S).  The magnitude is split
+// as hi * 2^32 + lo; hi * 2^32 + float(lo) is rounded once by the FMA and
+// float(lo) once before it, so the error is at most 2^7 units of the
+// fixed-point scale plus half an FP32 ulp of the result -- 2^-54 of the scale's
+// range bound 2^61, far below the FP32 resolution of any bin that matters --
+// and conversion is odd (-v converts to exactly minus v's value).  No FP64 or
+// 64-bit multiply instruction is involved.
+__device__ __forceinline__ float fix2f(long long v, float inv_scale) {
+    const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    const float r = fmaf(__uint2float_rn((unsigned)(a >> 32)), 4294967296.0f, __uint2float_rn((unsigned)a)) * inv_scale;
+    return v < 0 ? -r : r;
+}
+#endif
+
 }  // namespace bcsim_gb300

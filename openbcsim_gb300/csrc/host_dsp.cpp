@@ -41,7 +41,7 @@ void fft_double(std::vector<std::complex<double>>& x, int sign) {
     }
 }
 
-std::vector<std::complex<double>> analytic_pulse(const std::vector<float>& taps, int64_t M) {
+std::vector<std::complex<double>> analytic_spectrum(const std::vector<float>& taps, int64_t M) {
     std::vector<std::complex<double>> h(static_cast<size_t>(M), 0.0);
     for (size_t i = 0; i < taps.size() && static_cast<int64_t>(i) < M; i++) h[i] = taps[i];
     fft_double(h, -1);
@@ -57,6 +57,11 @@ std::vector<std::complex<double>> analytic_pulse(const std::vector<float>& taps,
         }
         h[i] *= k;
     }
+    return h;
+}
+
+std::vector<std::complex<double>> analytic_pulse(const std::vector<float>& taps, int64_t M) {
+    std::vector<std::complex<double>> h = analytic_spectrum(taps, M);
     fft_double(h, +1);
     for (auto& v : h) v /= static_cast<double>(M);
     return h;

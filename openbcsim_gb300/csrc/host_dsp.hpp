@@ -17,6 +17,9 @@ int64_t next_power_of_two(int64_t n);
 // In-place radix-2 FFT in double; sign -1 forward, +1 inverse (unscaled).
 void fft_double(std::vector<std::complex<double>>& x, int sign);
 
+// Analytic excitation spectrum FFT_M(taps) * hilbert_mask(M) (natural order).
+std::vector<std::complex<double>> analytic_spectrum(const std::vector<float>& taps, int64_t M);
+
 // Analytic excitation pulse h_a = IFFT(FFT_M(taps) * hilbert_mask(M))
 // (src/core/BeamConvolver.cpp:77-91, src/core/discrete_hilbert_mask.hpp:36-66).
 std::vector<std::complex<double>> analytic_pulse(const std::vector<float>& taps, int64_t M);

@@ -1,6 +1,7 @@
 // kernels.hpp -- structures shared by the host engine and the CUDA kernels, and
 // the host-side launchers of every kernel.
 #pragma once
+#include <complex>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -171,6 +172,25 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
                                        float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
                                        int max_ph_taps, int num_taps, int tap_start, int64_t M, int center,
                                        int decimation, int nd, const float2* demod, float2* out, cudaStream_t stream);
+
+// The same by FFT (fftconv.cu): the full length-M circular convolution with
+// the analytic pulse, one line per CTA in shared memory, for power-of-two
+// 256 <= M <= FFT_MAX_M.  spec/tw: the tables of make_fft_tables (M entries
+// each, 16-byte aligned).
+constexpr int64_t FFT_MAX_M = 16384;
+bool fft_convolution_supported(int64_t M);
+// F: the largest power of two dividing D, at most 16 (the decimation folded
+// into the spectrum); the shared memory of one CTA.
+int fft_fold(int D);
+size_t fft_convolution_smem(int64_t M, int D);
+// Host: H = FFT_M(h) * hilbert_mask in natural order (double) -> spec, the
+// spectrum in the forward transform's output order, times
+// exp(+j 2 pi center k / M) / M; tw[e] = exp(-j 2 pi e / M), e < M.
+void make_fft_tables(const std::complex<double>* H, int64_t M, int center, int D, float2* spec, float2* tw);
+cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
+                                           float inv_scale, const float2* spec, const float2* tw, int64_t M,
+                                           int decimation, int nd, const float2* demod, float2* out,
+                                           cudaStream_t stream);
 
 // Host: the FIR window taps[0..W) rearranged for the convolution kernel:
 // phase ph (0..D-1) holds, for t = 0, 1, ..., the tap w = W - 1 - (ph + t*D),

@@ -33,21 +33,70 @@ def run(job, mode="fp64", **params):
     return engine(job, mode, **params).simulate_lines_line_major()
 
 
+@pytest.mark.parametrize("conv", ["fir", "fft"])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_fp64_vs_oracle(oracle, name):
+def test_fp64_vs_oracle(oracle, name, conv):
     job, _ = load_golden(name)
-    iq = run(job)
+    iq = run(job, convolution=conv)
     ref = oracle.simulate(job, oracle.MODE_FP64)
     assert iq.shape == ref.shape
     assert oracle.rel_rms(iq, ref) <= FP64_TOL
 
 
+@pytest.mark.parametrize("conv", ["fir", "fft"])
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_reference_mode_vs_reference(oracle, name):
+def test_reference_mode_vs_reference(oracle, name, conv):
     job, z = load_golden(name)
-    iq = run(job, "reference")
+    iq = run(job, "reference", convolution=conv)
     assert oracle.rel_rms(iq, z["ref_iq"]) <= REF_IQ_TOL
     assert oracle.rel_rms(iq, oracle.simulate(job, oracle.MODE_REF32)) <= REF32_TOL
+
+
+def test_convolution_routes():
+    """The FFT route (the exact circular convolution) and the direct FIR (the
+    window of the analytic pulse holding all but 1e-10 of its energy) agree to
+    the window's truncation, about 1e-5; the automatic choice takes the FFT for
+    the long 2.5 MHz / bw 0.1 pulse (a ~2000-tap window) and the FIR for the
+    3.5 MHz / bw 0.15 pulse with decimation 8."""
+    from oracle.oracle import rel_rms
+
+    for name, route in (("sector_pd", "fft"), ("sector_nopd", "fft"), ("spline", "fft"), ("lut3d", "fir")):
+        job, _ = load_golden(name)
+        sim = engine(job)
+        assert sim.get_parameter("convolution_route") == ""
+        auto = sim.simulate_lines_line_major().copy()
+        assert sim.get_parameter("convolution_route") == route, name
+        fir = run(job, convolution="fir")
+        fft = run(job, convolution="fft")
+        assert np.array_equal(auto, fft if route == "fft" else fir)
+        assert rel_rms(fft, fir) <= 3e-5, name
+
+
+def test_fft_route_decimation_folds(oracle):
+    """Every decimation folds a different power of two into the spectrum
+    (F = 1, 2, 4, 8, 16; D = 48 folds 16 and keeps every third sample)."""
+    from openbcsim_gb300 import workloads as W
+
+    for D in (1, 2, 5, 12, 24, 32, 48):
+        job = W.sector_2d_fixed(num_scatterers=2000, num_lines=3, phase_delay=True, seed=40 + D)
+        job.decimation = D
+        iq = run(job, convolution="fft")
+        assert iq.shape == (3, -(-job.num_samples // D))
+        assert oracle.rel_rms(iq, oracle.simulate(job)) <= FP64_TOL, D
+
+
+def test_fft_route_rejects_long_lines():
+    """M beyond one CTA's shared memory: convolution=fft is refused, auto takes the FIR."""
+    from openbcsim_gb300 import workloads as W
+
+    job = W.sector_2d_fixed(num_scatterers=500, num_lines=2, phase_delay=True, seed=3)
+    s = job.scan
+    job.scan = type(s)(s.origins, s.directions, s.lateral_dirs, s.timestamps, 0.3)   # ns ~ 19.5k: M = 32768
+    with pytest.raises(RuntimeError, match="convolution=fft"):
+        run(job, convolution="fft")
+    sim = engine(job)
+    sim.simulate_lines_line_major()
+    assert sim.get_parameter("convolution_route") == "fir"
 
 
 @pytest.mark.parametrize("name", ["sector_pd", "lut3d", "spline", "linear"])
