@@ -26,16 +26,18 @@
 //      registers: with F the largest power of two dividing D (F <= 16), the
 //      samples y[F n'] are the length-M/F inverse transform of the spectrum
 //      folded onto k mod M/F, and the F terms of a fold lie in one thread's
-//      block of 16;
+//      block of 16 (the M/F results are written in place, after a barrier);
 //   3. inverse transform of length M/F, decimation in time: the exact inverse
 //      passes in reverse order, the last one writing out[m] = y[F n'] times
 //      the demodulation factor for the n' = m D / F.
 //
 // Shared memory holds the array padded by one float2 per 16 (element i at
 // i + i/16): every pass then reads and writes without bank conflicts (two
-// wavefronts per warp access of 8 bytes).  Twiddles W_M^e, e < M, come from a
-// host-made table (double precision rounded once), through the L1 cache.
-// FP32 throughout: the relative RMS error is ~2e-7 of the IQ.
+// wavefronts per warp access of 8 bytes).  It also holds a quarter-wave table
+// of twiddles W_M^y, y < M/4, copied from a host-made table (double precision
+// rounded once); a task reads four of them and multiplies out the rest.  M =
+// 8192 then takes 87 KB, two CTAs per SM; M = 16384 one.  FP32 throughout:
+// the relative RMS error is ~2e-7 of the IQ.
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -108,38 +110,60 @@ __device__ __forceinline__ void dft(float2 (&v)[R]) {
     }
 }
 
-// Twiddles W^(e q), q < R, of one task: the powers of two W^e, W^2e, W^4e,
-// W^8e from the table (tw[x] = W^x), the others as products of those (at most
-// three roundings deep: ~2e-7 relative).
+// W_M^x for 0 <= x < M/2 from the shared quarter-wave table tq (W_M^y, y < M/4,
+// padded like the data): W^(y + M/4) = -j W^y.
+__device__ __forceinline__ float2 twid(const float2* tq, int x, int q4) {
+    if (x < q4) return tq[fpad(x)];
+    const float2 a = tq[fpad(x - q4)];
+    return make_float2(a.y, -a.x);
+}
+
+// Twiddles W^(e q), 0 < q < R, of one task, held as six factors: W^e, W^2e,
+// W^3e = W^e W^2e for the two low bits of q, W^4e, W^8e, W^12e = W^4e W^8e for
+// the two high bits; W^(eq) is one factor or the product of one of each (at
+// most two roundings deep: ~2e-7 relative).  Twelve registers, not thirty.
+struct TaskTw {
+    float2 b1, b2, b3, b4, b8, b12;
+};
 template <int R>
-__device__ __forceinline__ void task_twiddles(const float2* __restrict__ tw, int e, float2 (&w)[R]) {
-    w[0] = make_float2(1.0f, 0.0f);
-#pragma unroll
-    for (int q = 1; q < R; q <<= 1) w[q] = __ldg(tw + e * q);
-#pragma unroll
-    for (int q = 3; q < R; q++)
-        if (q & (q - 1)) w[q] = cmul(w[q & -q], w[q - (q & -q)]);
+__device__ __forceinline__ TaskTw task_twiddles(const float2* tq, int q4, int e) {
+    TaskTw t;
+    t.b1 = twid(tq, e, q4);
+    if (R > 2) { t.b2 = twid(tq, 2 * e, q4); t.b3 = cmul(t.b1, t.b2); }
+    if (R > 4) t.b4 = twid(tq, 4 * e, q4);
+    if (R > 8) { t.b8 = twid(tq, 8 * e, q4); t.b12 = cmul(t.b4, t.b8); }
+    return t;
+}
+// y * W^(eq) (or y * conj W^(eq)), q a compile-time constant 0 < q < 16
+template <bool CONJ>
+__device__ __forceinline__ float2 twiddle_q(float2 y, int q, const TaskTw& t) {
+    const int lo = q & 3, hi = q >> 2;
+    const float2 wl = lo == 1 ? t.b1 : lo == 2 ? t.b2 : t.b3;
+    const float2 wh = hi == 1 ? t.b4 : hi == 2 ? t.b8 : t.b12;
+    const float2 w = lo == 0 ? wh : hi == 0 ? wl : cmul(wl, wh);
+    return CONJ ? cmul_conj(y, w) : cmul(y, w);
 }
 
 // One in-place pass of radix R over an array of Mc elements in blocks of
 // length L: forward (output q of offset n1 times W_L^(n1 q)) or its exact
-// inverse (input q times conj W_L^(n1 q), inverse DFT).  tw[e] = W_M^e; the
-// twiddle W_L^x is tw[x * ts], ts = M / L.  A thread takes 16 / R tasks at a
-// time, so that every pass keeps sixteen loads in flight per thread.
+// inverse (input q times conj W_L^(n1 q), inverse DFT).  The twiddle W_L^x is
+// W_M^(x ts), ts = M / L.  A thread takes 16 / R tasks at a time for R >= 8,
+// 8 / R below (eight or sixteen loads in flight per thread).
 template <int R, bool INV>
-__device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const float2* __restrict__ tw) {
-    constexpr int G = 16 / R;
+__device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const float2* tq, int q4) {
+    constexpr int G = R >= 8 ? 16 / R : 8 / R;
     const int S = L / R;
     const int T = Mc / R;
     for (int t0 = threadIdx.x; t0 < T; t0 += blockDim.x * G) {
-        float2 v[G][R], w[G][R];
+        float2 v[G][R];
+        TaskTw w[G];
         int base[G];
 #pragma unroll
         for (int g = 0; g < G; g++) {
             const int t = min(t0 + g * (int)blockDim.x, T - 1);   // (a clamped task is recomputed, not stored)
             const int n1 = t & (S - 1);
             base[g] = (t - n1) * R + n1;
-            task_twiddles<R>(tw, n1 * ts, w[g]);
+            w[g] = task_twiddles<R>(tq, q4, n1 * ts);
 #pragma unroll
             for (int j = 0; j < R; j++) v[g][j] = s[fpad(base[g] + j * S)];
         }
@@ -147,7 +171,7 @@ __device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const
         for (int g = 0; g < G; g++) {
             if (INV) {
 #pragma unroll
-                for (int q = 1; q < R; q++) v[g][q] = cmul_conj(v[g][q], w[g][q]);
+                for (int q = 1; q < R; q++) v[g][q] = twiddle_q<true>(v[g][q], q, w[g]);
             }
             dft<R, INV>(v[g]);
         }
@@ -157,7 +181,7 @@ __device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const
 #pragma unroll
             for (int q = 0; q < R; q++) {
                 float2 y = v[g][bit_reverse(q, R)];
-                if (!INV && q > 0) y = cmul(y, w[g][q]);
+                if (!INV && q > 0) y = twiddle_q<false>(y, q, w[g]);
                 s[fpad(base[g] + q * S)] = y;
             }
         }
@@ -166,26 +190,41 @@ __device__ __forceinline__ void fft_pass(float2* s, int Mc, int L, int ts, const
 
 // The fused middle: last forward pass (blocks of 16, no twiddles), multiply by
 // the spectrum, fold by F = 16 / RF, first inverse pass (radix RF, blocks of
-// RF, no twiddles), into dst (dst == s when RF == 16: same positions).
-template <int RF>
-__device__ __forceinline__ void fft_middle(const float2* s, float2* dst, int M, const float4* __restrict__ spec4) {
-    for (int b = threadIdx.x; b < M / 16; b += blockDim.x) {
+// RF, no twiddles), in place: block b's RF results go to b*RF .. b*RF+RF-1
+// after every thread has read its blocks (at most two per thread).
+template <int RF, int NB>
+__device__ __forceinline__ void fft_middle(float2* s, int M, const float4* __restrict__ spec4) {
+    float2 f[NB][RF];
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        const int b = threadIdx.x + i * blockDim.x;
+        if (b >= M / 16) break;
         float2 v[16];
 #pragma unroll
         for (int j = 0; j < 16; j++) v[j] = s[fpad(b * 16 + j)];
         dft<16, false>(v);
-        float2 f[RF];
 #pragma unroll
-        for (int r = 0; r < RF; r++) f[r] = make_float2(0.0f, 0.0f);
+        for (int r = 0; r < RF; r++) f[i][r] = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int q = 0; q < 16; q += 2) {
             const float4 h = __ldg(spec4 + b * 8 + q / 2);   // spectrum entries q, q + 1
-            f[q % RF] = cadd(f[q % RF], cmul(v[bit_reverse(q, 16)], make_float2(h.x, h.y)));
-            f[(q + 1) % RF] = cadd(f[(q + 1) % RF], cmul(v[bit_reverse(q + 1, 16)], make_float2(h.z, h.w)));
+            f[i][q % RF] = cadd(f[i][q % RF], cmul(v[bit_reverse(q, 16)], make_float2(h.x, h.y)));
+            f[i][(q + 1) % RF] = cadd(f[i][(q + 1) % RF], cmul(v[bit_reverse(q + 1, 16)], make_float2(h.z, h.w)));
         }
-        if (RF > 1) dft<RF, true>(f);
+        if (RF > 1) dft<RF, true>(f[i]);
+        if (RF == 16) {   // no fold: the block's own positions
 #pragma unroll
-        for (int k = 0; k < RF; k++) dst[fpad(b * RF + k)] = f[bit_reverse(k, RF)];
+            for (int k = 0; k < RF; k++) s[fpad(b * RF + k)] = f[i][bit_reverse(k, RF)];
+        }
+    }
+    if (RF == 16) return;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NB; i++) {
+        const int b = threadIdx.x + i * blockDim.x;
+        if (b >= M / 16) break;
+#pragma unroll
+        for (int k = 0; k < RF; k++) s[fpad(b * RF + k)] = f[i][bit_reverse(k, RF)];
     }
 }
 
@@ -212,7 +251,11 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
     extern __shared__ __align__(16) float2 fsm[];
     float2* s = fsm;
     const int Mp = M / F;
-    float2* s2 = F > 1 ? fsm + fpad(M) : fsm;
+    float2* s2 = fsm;
+    float2* tq = fsm + fpad(M);   // W_M^y, y < M/4
+    const int q4 = M / 4;
+    for (int y = threadIdx.x; y < q4; y += blockDim.x) tq[fpad(y)] = __ldg(tw + y);
+    __syncthreads();
     const int line = blockIdx.x;
     const long long* lb = reinterpret_cast<const long long*>(bins) + (int64_t)line * ns * (PD ? 2 : 1);
 
@@ -221,15 +264,15 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
     {
         const int S = M / 16;
         for (int t = threadIdx.x; t < S; t += blockDim.x) {
-            float2 v[16], w[16];
-            task_twiddles<16>(tw, t, w);
+            float2 v[16];
+            const TaskTw w = task_twiddles<16>(tq, q4, t);
 #pragma unroll
             for (int j = 0; j < 16; j++) v[j] = load_bin<PD>(lb, t + j * S, ns, inv_scale);
             dft<16, false>(v);
 #pragma unroll
             for (int q = 0; q < 16; q++) {
                 float2 y = v[bit_reverse(q, 16)];
-                if (q > 0) y = cmul(y, w[q]);
+                if (q > 0) y = twiddle_q<false>(y, q, w);
                 s[fpad(t + q * S)] = y;
             }
         }
@@ -237,28 +280,28 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
     __syncthreads();
     int L = M / 16;
     if (RS > 1) {
-        fft_pass<RS, false>(s, M, L, M / L, tw);
+        fft_pass<RS, false>(s, M, L, M / L, tq, q4);
         __syncthreads();
         L /= RS;
     }
     for (; L > 16; L /= 16) {
-        fft_pass<16, false>(s, M, L, M / L, tw);
+        fft_pass<16, false>(s, M, L, M / L, tq, q4);
         __syncthreads();
     }
     switch (F) {
-        case 1: fft_middle<16>(s, s2, M, spec4); break;
-        case 2: fft_middle<8>(s, s2, M, spec4); break;
-        case 4: fft_middle<4>(s, s2, M, spec4); break;
-        case 8: fft_middle<2>(s, s2, M, spec4); break;
-        default: fft_middle<1>(s, s2, M, spec4); break;
+        case 1: fft_middle<16, MINB == 2 ? 1 : 2>(s, M, spec4); break;
+        case 2: fft_middle<8, MINB == 2 ? 1 : 2>(s, M, spec4); break;
+        case 4: fft_middle<4, MINB == 2 ? 1 : 2>(s, M, spec4); break;
+        case 8: fft_middle<2, MINB == 2 ? 1 : 2>(s, M, spec4); break;
+        default: fft_middle<1, MINB == 2 ? 1 : 2>(s, M, spec4); break;
     }
     __syncthreads();
     for (L = (16 / F) * 16; L <= Mp / (16 * RS); L *= 16) {
-        fft_pass<16, true>(s2, Mp, L, M / L, tw);
+        fft_pass<16, true>(s2, Mp, L, M / L, tq, q4);
         __syncthreads();
     }
     if (RS > 1) {
-        fft_pass<RS, true>(s2, Mp, Mp / 16, M / (Mp / 16), tw);
+        fft_pass<RS, true>(s2, Mp, Mp / 16, M / (Mp / 16), tq, q4);
         __syncthreads();
     }
     // output pass (radix 16, L' = M'): samples y[F n'], n' = k1 + k2 M'/16;
@@ -267,12 +310,12 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
         const int S = Mp / 16;
         const int DF = D / F;
         for (int k1 = threadIdx.x; k1 < S; k1 += blockDim.x) {
-            float2 v[16], w[16];
-            task_twiddles<16>(tw, k1 * F, w);
+            float2 v[16];
+            const TaskTw w = task_twiddles<16>(tq, q4, k1 * F);
 #pragma unroll
             for (int q = 0; q < 16; q++) v[q] = s2[fpad(k1 + q * S)];
 #pragma unroll
-            for (int q = 1; q < 16; q++) v[q] = cmul_conj(v[q], w[q]);
+            for (int q = 1; q < 16; q++) v[q] = twiddle_q<true>(v[q], q, w);
             dft<16, true>(v);
 #pragma unroll
             for (int k = 0; k < 16; k++) {
@@ -303,7 +346,8 @@ int fft_fold(int D) {
 
 size_t fft_convolution_smem(int64_t M, int D) {
     const int64_t F = fft_fold(D);
-    const int64_t words = (M + M / 16) + (F > 1 ? (M / F + M / F / 16) : 0);
+    (void)F;
+    const int64_t words = (M + M / 16) + (M / 4 + M / 64);
     return (size_t)words * sizeof(float2);
 }
 
