@@ -500,11 +500,11 @@ std::vector<double> Simulator::get_debug_data(const std::string& key) const {
 // complex MACs per line, the FFT route two transforms of M points (the inverse
 // shortened by the decimation fold); the FIR wins for short windows.
 // Measured on GB300: the FIR costs ~0.23 ns per line per output-tap, the FFT
-// route ~1.3 ns per line per M log2 M.
+// route ~0.75-1.0 ns per line per M log2 M.
 static bool fft_preferred(int64_t M, int64_t nd, int64_t window) {
     int lg = 0;
     while ((int64_t(1) << lg) < M) lg++;
-    return (double)nd * (double)window > 6.0 * (double)M * (double)lg;
+    return (double)nd * (double)window > 4.0 * (double)M * (double)lg;
 }
 
 void Simulator::prepare_excitation_tables() {

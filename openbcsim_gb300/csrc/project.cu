@@ -422,7 +422,6 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     // one bin and one fold group (the walk folds and stores only at their ends)
     __shared__ int s_seg[1024 + 2];
     __shared__ int s_seg_warp[32];
-    __shared__ int s_nseg;
     const int n_valid = __ldg(counts);
     const int64_t start = (int64_t)blockIdx.x * chunk;
     if (start >= n_valid) return;
@@ -540,11 +539,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         }
         if (tid == 0) {
             s_seg[total] = cnt;
-            s_nseg = total;
         }
         __syncthreads();
     }
-    const int nseg = s_nseg;
 
     for (int g0 = 0; g0 < L; g0 += blockDim.x) {
         if (g0 + (tid & ~31) >= L) break;   // this warp has no line in this group (nor in later ones)
@@ -576,8 +573,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 bool pass = false, sure = true;
                 if (r < cnt) {
                     const float4 A = smA[r];
-                    const float u = fmaf(A.z, lz, fmaf(A.y, ly, A.x * lx));
-                    const float v = fmaf(A.z, ez, fmaf(A.y, ey, A.x * ex));
+                    const float2 uv = __ffma2_rn(make_float2(A.z, A.z), make_float2(lz, ez),
+                                      __ffma2_rn(make_float2(A.y, A.y), make_float2(ly, ey),
+                                      __fmul2_rn(make_float2(A.x, A.x), make_float2(lx, ex))));
+                    const float u = uv.x, v = uv.y;
                     const float dt = fmaf(A.z, rz, fmaf(A.y, ry, A.x * rx));
                     // |A|^2, and |A_perp|^2 = |A|^2 - dt^2 bounded from above: the
                     // margin 4e-6 |A|^2 exceeds the rounding of both terms and of the
@@ -675,8 +674,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                         w8 = signbit(dot) ? 0.0f : w8;
                     } else {
                         const float dot = NODOT ? 1.0f : fmaf(A.z, q.rz, fmaf(A.y, q.ry, A.x * q.rx));
-                        const float u = fmaf(A.z, q.uz, fmaf(A.y, q.uy, fmaf(A.x, q.ux, q.ou)));
-                        const float v = fmaf(A.z, q.vz, fmaf(A.y, q.vy, fmaf(A.x, q.vx, q.ov)));
+                        const float2 uv = __ffma2_rn(make_float2(A.z, A.z), make_float2(q.uz, q.vz),
+                                          __ffma2_rn(make_float2(A.y, A.y), make_float2(q.uy, q.vy),
+                                          __ffma2_rn(make_float2(A.x, A.x), make_float2(q.ux, q.vx), make_float2(q.ou, q.ov))));
+                        const float u = uv.x, v = uv.y;
                         if (BEAM == BEAM_GAUSSIAN) {
                             w8 = exp2f(-fmaf(u, u, v * v));
                             // arc projection: a line for which the scatterer lies behind the
