@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "scatterer-line projections/s"
 # DRAM traffic of one projection launch of the default workloads (ncu, full size)
-NCU_TRAFFIC_BYTES = {"volume_3d_lut": 395.58e6 + 354.83e6}
+NCU_TRAFFIC_BYTES = {"volume_3d_lut": 395.99e6 + 354.79e6}
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
