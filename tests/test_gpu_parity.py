@@ -85,6 +85,27 @@ def test_fft_route_decimation_folds(oracle):
         assert oracle.rel_rms(iq, oracle.simulate(job)) <= FP64_TOL, D
 
 
+@pytest.mark.parametrize("line_length,fc,bw,D", [(0.0019, 3.5e6, 0.15, 8), (0.0036, 2.5e6, 0.1, 10),
+                                                (0.006, 2.5e6, 0.1, 10), (0.012, 2.5e6, 0.1, 5),
+                                                (0.05, 2.5e6, 0.1, 16)])
+def test_fft_route_transform_lengths(oracle, line_length, fc, bw, D):
+    """Transform lengths M = 256, 512, 1024, 2048, 4096: every radix plan of the
+    FFT route (16 x 16, 16 x 2 x 16, 16 x 4 x 16, 16 x 8 x 16, 16 x 16 x 16)
+    against the FP64 oracle, scatterers within the short lines."""
+    from openbcsim_gb300 import workloads as W
+
+    rng = np.random.default_rng(int(line_length * 1e5))
+    n = 3000
+    xyza = np.stack([rng.uniform(-0.3, 0.3, n) * line_length, np.zeros(n),
+                     rng.uniform(0.1, 0.95, n) * line_length, rng.standard_normal(n)], axis=1).astype(np.float32)
+    scan = W.sector_scan(4, 20.0, line_length)
+    job = W._excitation_job("short_lines", scan, fc, bw, W.GaussianBeam(1e-3, 1e-3), [W.FixedSet(xyza)], [], D)
+    iq = run(job, convolution="fft")
+    M = 1 << int(np.ceil(np.log2(job.num_samples + len(job.taps) - 1)))
+    assert M <= 4096 and np.abs(iq).max() > 0
+    assert oracle.rel_rms(iq, oracle.simulate(job)) <= FP64_TOL, M
+
+
 def test_fft_route_rejects_long_lines():
     """M beyond one CTA's shared memory: convolution=fft is refused, auto takes the FIR."""
     from openbcsim_gb300 import workloads as W
