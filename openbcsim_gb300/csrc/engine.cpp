@@ -258,7 +258,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "fir_tail_energy") return fmt_double(fir_tail_);
     if (key == "convolution") return convolution_ == 0 ? "auto" : convolution_ == 1 ? "fir" : "fft";
     // the route the last prepared configuration took ("" before the first simulation)
-    if (key == "convolution_route") return tables_valid_ ? (use_fft_ ? "fft" : "fir") : "";
+    if (key == "convolution_route") return route_known_ ? (last_route_fft_ ? "fft" : "fir") : "";
     if (key == "tile_lines") return std::to_string(tile_lines_);
     if (key == "cull") return cull_ ? "on" : "off";
     if (key == "record_cache") return record_cache_ ? "on" : "off";
@@ -496,15 +496,20 @@ std::vector<double> Simulator::get_debug_data(const std::string& key) const {
 // derived tables
 // ---------------------------------------------------------------------------
 
-// Automatic convolution route: the direct FIR evaluates nd outputs of `window`
-// complex MACs per line, the FFT route two transforms of M points (the inverse
-// shortened by the decimation fold); the FIR wins for short windows.
-// Measured on GB300: the FIR costs ~0.23 ns per line per output-tap, the FFT
-// route ~0.75-1.0 ns per line per M log2 M.
-static bool fft_preferred(int64_t M, int64_t nd, int64_t window) {
+// Automatic convolution route, from the time each takes on GB300 for L lines:
+// the direct FIR ~0.23 ps per line, output and tap plus ~8 us, filling the GPU
+// at any line count (a line's outputs split over more CTAs when lines are
+// few); the FFT route one CTA per line, a wave of 2 CTAs per SM (M <= 8192,
+// ~30 us at M = 8192, scaling with M log2 M) or 1 (M = 16384, ~25 us).  Few
+// lines or short windows favour the FIR.
+static bool fft_faster(int64_t L, int64_t nd, int64_t window, int64_t M, int sms) {
     int lg = 0;
     while ((int64_t(1) << lg) < M) lg++;
-    return (double)nd * (double)window > 4.0 * (double)M * (double)lg;
+    const double t_fir = (double)L * (double)nd * (double)window * 0.23e-12 + 8e-6;
+    const int64_t slots = (M <= 8192 ? 2 : 1) * (int64_t)std::max(sms, 1);
+    const double t_wave = M <= 8192 ? 30e-6 * (double)M * lg / (8192.0 * 13.0) : 25e-6;
+    const double t_fft = (double)((L + slots - 1) / slots) * t_wave;
+    return t_fft < t_fir;
 }
 
 void Simulator::prepare_excitation_tables() {
@@ -546,18 +551,17 @@ void Simulator::prepare_excitation_tables() {
     ph_off_dev_.reserve(off.size() * sizeof(int), stream_);
     BCSIM_CUDA(cudaMemcpyAsync(taps_pm_dev_.get(), pm.data(), (size_t)ntaps_pm_ * sizeof(float2), cudaMemcpyHostToDevice, stream_));
     BCSIM_CUDA(cudaMemcpyAsync(ph_off_dev_.get(), off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
-    // convolution route: the FFT when its line fits one CTA's shared memory and
-    // it costs less than the direct FIR's nd * window complex MACs per line
+    // the FFT route, where a line fits one CTA's shared memory; its tables
+    // depend on the excitation, M and the center only (not on the decimation)
     int smem_optin = 0;
     BCSIM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
-    const bool fft_ok = fft_convolution_supported(M_) && ns_ <= M_ &&
-                        fft_convolution_smem(M_, decimation_) <= (size_t)smem_optin;
-    if (convolution_ == 2 && !fft_ok)
+    BCSIM_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_));
+    fft_ok_ = fft_convolution_supported(M_) && ns_ <= M_ && fft_convolution_smem(M_, decimation_) <= (size_t)smem_optin;
+    if (convolution_ == 2 && !fft_ok_)
         throw SimError(BCSIM_E_INVALID, "convolution=fft needs a power-of-two convolution length M in [256, 16384] "
                                         "(this configuration has M = " + std::to_string(M_) + ")");
-    use_fft_ = convolution_ == 2 || (convolution_ == 0 && fft_ok && fft_preferred(M_, nd_, tap_count_));
     std::vector<float2> hold_spec, hold_tw;
-    if (use_fft_) {
+    if (convolution_ != 1 && fft_ok_ && !(fft_key_taps_ == taps_ && fft_key_M_ == M_ && fft_key_center_ == center_)) {
         hold_spec.resize((size_t)M_);
         hold_tw.resize((size_t)M_);
         make_fft_tables(analytic_spec_.data(), M_, center_, decimation_, hold_spec.data(), hold_tw.data());
@@ -567,6 +571,9 @@ void Simulator::prepare_excitation_tables() {
                                    cudaMemcpyHostToDevice, stream_));
         BCSIM_CUDA(cudaMemcpyAsync(fft_tw_dev_.get(), hold_tw.data(), (size_t)M_ * sizeof(float2),
                                    cudaMemcpyHostToDevice, stream_));
+        fft_key_taps_ = taps_;
+        fft_key_M_ = M_;
+        fft_key_center_ = center_;
     }
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
     tables_valid_ = true;
@@ -1267,6 +1274,9 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     // convolution + demodulation + decimation; with a host destination in
     // blocks of lines, each block's IQ copied out while the next is convolved
     timer.restart();
+    const bool use_fft = convolution_ == 2 || (convolution_ == 0 && fft_ok_ && fft_faster(L, nd_, tap_count_, M_, sms_));
+    last_route_fft_ = use_fft;
+    route_known_ = true;
     const int nblocks = (host_out && L >= 1024) ? 4 : 1;
     while ((int)ev_blocks_.size() < nblocks) {
         cudaEvent_t e = nullptr;
@@ -1278,7 +1288,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         const int l0 = (int)((int64_t)L * k / nblocks), l1 = (int)((int64_t)L * (k + 1) / nblocks);
         if (l1 <= l0) continue;
         ++launches;
-        if (use_fft_)
+        if (use_fft)
             BCSIM_CUDA(launch_fft_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns,
                                                       p.phase_delay, std::ldexp(1.0f, -p.log2scale),
                                                       fft_spec_dev_.as<float2>(), fft_tw_dev_.as<float2>(), M_,
@@ -1473,6 +1483,7 @@ void Simulator::clone_from(Simulator& o) {
     threads_per_block_ = o.threads_per_block_;
     mode_ = o.mode_;
     fir_tail_ = o.fir_tail_;
+    convolution_ = o.convolution_;
     tile_lines_ = o.tile_lines_;
     cull_ = o.cull_;
     record_cache_ = o.record_cache_;

@@ -285,8 +285,14 @@ private:
     DeviceBuffer demod_dev_, taps_pm_dev_, ph_off_dev_;
     std::vector<float2> fir_taps_host_;   // the FIR window taps, in window order
     std::vector<std::complex<double>> analytic_spec_;   // FFT_M(h) * hilbert mask, for the FFT route
-    bool use_fft_ = false;   // convolution by FFT (fftconv.cu) rather than the direct FIR
-    DeviceBuffer fft_spec_dev_, fft_tw_dev_;
+    bool fft_ok_ = false;          // the FFT route (fftconv.cu) fits this configuration
+    bool last_route_fft_ = false;  // the route the last simulation took
+    bool route_known_ = false;
+    int sms_ = 0;
+    DeviceBuffer fft_spec_dev_, fft_tw_dev_;   // its tables, for fft_key_*
+    std::vector<float> fft_key_taps_;
+    int64_t fft_key_M_ = -1;
+    int fft_key_center_ = -1;
     int ntaps_pm_ = 0, max_ph_taps_ = 0;
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;

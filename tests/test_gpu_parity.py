@@ -55,21 +55,24 @@ def test_reference_mode_vs_reference(oracle, name, conv):
 def test_convolution_routes():
     """The FFT route (the exact circular convolution) and the direct FIR (the
     window of the analytic pulse holding all but 1e-10 of its energy) agree to
-    the window's truncation, about 1e-5; the automatic choice takes the FFT for
-    the long 2.5 MHz / bw 0.1 pulse (a ~2000-tap window) and the FIR for the
-    3.5 MHz / bw 0.15 pulse with decimation 8."""
+    the window's truncation, about 1e-5.  The automatic choice weighs the two
+    routes' times for the line count: the FFT (one CTA per line) for many lines
+    with the long 2.5 MHz / bw 0.1 pulse (a 1960-tap window), the FIR for few
+    lines and for the short 3.5 MHz / bw 0.15 pulse with decimation 8."""
     from oracle.oracle import rel_rms
+    from openbcsim_gb300 import workloads as W
 
-    for name, route in (("sector_pd", "fft"), ("sector_nopd", "fft"), ("spline", "fft"), ("lut3d", "fir")):
-        job, _ = load_golden(name)
+    many = W.sector_2d_fixed(num_scatterers=2000, num_lines=256, phase_delay=True, seed=17)
+    cases = [(load_golden("sector_pd")[0], "fir"), (load_golden("lut3d")[0], "fir"), (many, "fft")]
+    for job, route in cases:
         sim = engine(job)
         assert sim.get_parameter("convolution_route") == ""
         auto = sim.simulate_lines_line_major().copy()
-        assert sim.get_parameter("convolution_route") == route, name
+        assert sim.get_parameter("convolution_route") == route, job.name
         fir = run(job, convolution="fir")
         fft = run(job, convolution="fft")
         assert np.array_equal(auto, fft if route == "fft" else fir)
-        assert rel_rms(fft, fir) <= 3e-5, name
+        assert rel_rms(fft, fir) <= 3e-5, job.name
 
 
 def test_fft_route_decimation_folds(oracle):
