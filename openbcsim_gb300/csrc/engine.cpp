@@ -556,7 +556,7 @@ void Simulator::prepare_excitation_tables() {
     int smem_optin = 0;
     BCSIM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
     BCSIM_CUDA(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_));
-    fft_ok_ = fft_convolution_supported(M_) && ns_ <= M_ && fft_convolution_smem(M_, decimation_) <= (size_t)smem_optin;
+    fft_ok_ = fft_convolution_supported(M_) && ns_ <= M_ && fft_convolution_smem(M_) <= (size_t)smem_optin;
     if (convolution_ == 2 && !fft_ok_)
         throw SimError(BCSIM_E_INVALID, "convolution=fft needs a power-of-two convolution length M in [256, 16384] "
                                         "(this configuration has M = " + std::to_string(M_) + ")");
@@ -564,7 +564,7 @@ void Simulator::prepare_excitation_tables() {
     if (convolution_ != 1 && fft_ok_ && !(fft_key_taps_ == taps_ && fft_key_M_ == M_ && fft_key_center_ == center_)) {
         hold_spec.resize((size_t)M_);
         hold_tw.resize((size_t)M_);
-        make_fft_tables(analytic_spec_.data(), M_, center_, decimation_, hold_spec.data(), hold_tw.data());
+        make_fft_tables(analytic_spec_.data(), M_, center_, hold_spec.data(), hold_tw.data());
         fft_spec_dev_.reserve((size_t)M_ * sizeof(float2), stream_);
         fft_tw_dev_.reserve((size_t)M_ * sizeof(float2), stream_);
         BCSIM_CUDA(cudaMemcpyAsync(fft_spec_dev_.get(), hold_spec.data(), (size_t)M_ * sizeof(float2),

@@ -134,6 +134,17 @@ __device__ __forceinline__ TaskTw task_twiddles(const float2* tq, int q4, int e)
     if (R > 8) { t.b8 = twid(tq, 8 * e, q4); t.b12 = cmul(t.b4, t.b8); }
     return t;
 }
+// the same from the global table (tw[x] = W_M^x, x < M)
+__device__ __forceinline__ TaskTw task_twiddles_global(const float2* __restrict__ tw, int e) {
+    TaskTw t;
+    t.b1 = __ldg(tw + e);
+    t.b2 = __ldg(tw + 2 * e);
+    t.b4 = __ldg(tw + 4 * e);
+    t.b8 = __ldg(tw + 8 * e);
+    t.b3 = cmul(t.b1, t.b2);
+    t.b12 = cmul(t.b4, t.b8);
+    return t;
+}
 // y * W^(eq) (or y * conj W^(eq)), q a compile-time constant 0 < q < 16
 template <bool CONJ>
 __device__ __forceinline__ float2 twiddle_q(float2 y, int q, const TaskTw& t) {
@@ -248,24 +259,21 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
     fft_convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale, int M,
                                    int F, const float4* __restrict__ spec4, const float2* __restrict__ tw, int D,
                                    int nd, const float2* __restrict__ demod, float2* __restrict__ out) {
-    extern __shared__ __align__(16) float2 fsm[];
-    float2* s = fsm;
+    extern __shared__ __align__(16) float2 s[];
     const int Mp = M / F;
-    float2* s2 = fsm;
-    float2* tq = fsm + fpad(M);   // W_M^y, y < M/4
+    float2* tq = s + fpad(M);   // W_M^y, y < M/4 (complete at the barrier after pass 0)
     const int q4 = M / 4;
     for (int y = threadIdx.x; y < q4; y += blockDim.x) tq[fpad(y)] = __ldg(tw + y);
-    __syncthreads();
     const int line = blockIdx.x;
     const long long* lb = reinterpret_cast<const long long*>(bins) + (int64_t)line * ns * (PD ? 2 : 1);
 
     // forward pass 0 (radix 16, L = M), from the bins: sixteen independent
-    // loads per task
+    // loads per task, its twiddles from the global table meanwhile
     {
         const int S = M / 16;
         for (int t = threadIdx.x; t < S; t += blockDim.x) {
             float2 v[16];
-            const TaskTw w = task_twiddles<16>(tq, q4, t);
+            const TaskTw w = task_twiddles_global(tw, t);
 #pragma unroll
             for (int j = 0; j < 16; j++) v[j] = load_bin<PD>(lb, t + j * S, ns, inv_scale);
             dft<16, false>(v);
@@ -297,11 +305,11 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
     }
     __syncthreads();
     for (L = (16 / F) * 16; L <= Mp / (16 * RS); L *= 16) {
-        fft_pass<16, true>(s2, Mp, L, M / L, tq, q4);
+        fft_pass<16, true>(s, Mp, L, M / L, tq, q4);
         __syncthreads();
     }
     if (RS > 1) {
-        fft_pass<RS, true>(s2, Mp, Mp / 16, M / (Mp / 16), tq, q4);
+        fft_pass<RS, true>(s, Mp, Mp / 16, M / (Mp / 16), tq, q4);
         __syncthreads();
     }
     // output pass (radix 16, L' = M'): samples y[F n'], n' = k1 + k2 M'/16;
@@ -313,7 +321,7 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
             float2 v[16];
             const TaskTw w = task_twiddles<16>(tq, q4, k1 * F);
 #pragma unroll
-            for (int q = 0; q < 16; q++) v[q] = s2[fpad(k1 + q * S)];
+            for (int q = 0; q < 16; q++) v[q] = s[fpad(k1 + q * S)];
 #pragma unroll
             for (int q = 1; q < 16; q++) v[q] = twiddle_q<true>(v[q], q, w);
             dft<16, true>(v);
@@ -344,14 +352,12 @@ int fft_fold(int D) {
     return F;
 }
 
-size_t fft_convolution_smem(int64_t M, int D) {
-    const int64_t F = fft_fold(D);
-    (void)F;
+size_t fft_convolution_smem(int64_t M) {
     const int64_t words = (M + M / 16) + (M / 4 + M / 64);
     return (size_t)words * sizeof(float2);
 }
 
-void make_fft_tables(const std::complex<double>* H, int64_t M, int center, int D, float2* spec, float2* tw) {
+void make_fft_tables(const std::complex<double>* H, int64_t M, int center, float2* spec, float2* tw) {
     // position p of the forward transform's output holds frequency
     // k = q_0 + R_0 (q_1 + R_1 (q_2 + ...)), p = q_0 M/R_0 + q_1 M/(R_0 R_1) + ...
     std::vector<int> radices{16};
@@ -377,7 +383,6 @@ void make_fft_tables(const std::complex<double>* H, int64_t M, int center, int D
         const double ph = -two_pi * (double)e / (double)M;
         tw[e] = make_float2((float)std::cos(ph), (float)std::sin(ph));
     }
-    (void)D;
 }
 
 cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
@@ -387,7 +392,7 @@ cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int n
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
     if (!fft_convolution_supported(M) || ns > M) return cudaErrorInvalidValue;
     const int F = fft_fold(decimation);
-    const size_t smem = fft_convolution_smem(M, decimation);
+    const size_t smem = fft_convolution_smem(M);
     const int RS = fft_mid_radix(M);
     const bool two = 2 * smem <= 227 * 1024;   // two CTAs per SM fit: leave them the registers
     auto launch = [&](auto k) -> cudaError_t {

@@ -182,11 +182,11 @@ bool fft_convolution_supported(int64_t M);
 // F: the largest power of two dividing D, at most 16 (the decimation folded
 // into the spectrum); the shared memory of one CTA.
 int fft_fold(int D);
-size_t fft_convolution_smem(int64_t M, int D);
+size_t fft_convolution_smem(int64_t M);
 // Host: H = FFT_M(h) * hilbert_mask in natural order (double) -> spec, the
 // spectrum in the forward transform's output order, times
 // exp(+j 2 pi center k / M) / M; tw[e] = exp(-j 2 pi e / M), e < M.
-void make_fft_tables(const std::complex<double>* H, int64_t M, int center, int D, float2* spec, float2* tw);
+void make_fft_tables(const std::complex<double>* H, int64_t M, int center, float2* spec, float2* tw);
 cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                            float inv_scale, const float2* spec, const float2* tw, int64_t M,
                                            int decimation, int nd, const float2* demod, float2* out,
