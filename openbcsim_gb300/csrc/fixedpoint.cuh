@@ -10,6 +10,7 @@
 // the C library's conversions.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -71,6 +72,30 @@ BCSIM_HD long long f2ll_rn(float x) {
         mag = q + ((rem > half || (rem == half && (q & 1u))) ? 1u : 0u);
     }
     return (u >> 31) ? -(long long)mag : (long long)mag;
+}
+
+// float -> int64, rounding to nearest even, for |x| < 2^62 (a bin
+// contribution: the fixed-point scale keeps every sum below 2^61); other
+// values take f2ll_rn.  Below 2^31 one FP32 -> int32 conversion; above, x is
+// an integer: x = h 2^32 + l with h = floor(x / 2^32) and l = x - h 2^32 both
+// exact in FP32 (l < 2^32 has at most 24 significant bits), each converted
+// exactly.  Three to five instructions instead of the integer code's ~18.
+BCSIM_HD long long f2ll_rn_bounded(float x) {
+#if defined(__CUDA_ARCH__)
+    const float ax = fabsf(x);
+    if (ax < 2147483648.0f) return (long long)__float2int_rn(x);
+    if (!(ax < 4.611686e18f)) return f2ll_rn(x);
+    const float h = floorf(x * 2.3283064365386963e-10f);
+    const float l = fmaf(-h, 4294967296.0f, x);
+    return (long long)__float2int_rn(h) * 4294967296ll + (long long)__float2uint_rn(l);
+#else
+    const float ax = std::fabs(x);
+    if (ax < 2147483648.0f) return (long long)std::nearbyint(x);
+    if (!(ax < 4.611686e18f)) return f2ll_rn(x);
+    const float h = std::floor(x * 2.3283064365386963e-10f);
+    const float l = std::fma(-h, 4294967296.0f, x);
+    return (long long)h * 4294967296ll + (long long)l;
+#endif
 }
 
 // int64 -> float, rounding to nearest even.

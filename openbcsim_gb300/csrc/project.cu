@@ -43,7 +43,7 @@ static constexpr double TWO_PI_LITERAL = 6.283185307179586;  // CpuAlgorithm.cpp
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void bin_add(unsigned long long* addr, float v, float scale) {
     if (v != 0.0f) {
-        const long long q = f2ll_rn(v * scale);
+        const long long q = f2ll_rn_bounded(v * scale);
         if (q != 0) atomicAdd(addr, (unsigned long long)q);
     }
 }

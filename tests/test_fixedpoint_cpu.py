@@ -1,8 +1,9 @@
-"""The integer-only FP32 <-> int64 conversions used by the projection folds and
-the FIR staging (openbcsim_gb300/csrc/fixedpoint.cuh) round exactly like the
-C library's round-to-nearest-even conversions (llrintf and the int64 -> float
-cast), over edge values and random bit patterns.  The functions are plain
-integer C++, compiled here for the host."""
+"""The FP32 <-> int64 conversions used by the projection folds, the per-pair
+atomics and the FIR staging (openbcsim_gb300/csrc/fixedpoint.cuh) round exactly
+like the C library's round-to-nearest-even conversions (llrintf and the int64
+-> float cast), over edge values and random bit patterns.  The functions are
+plain C++ compiled here for the host (the bounded conversion's device form
+swaps nearbyint/floor/fma for the CUDA intrinsics of the same rounding)."""
 import os
 import subprocess
 
@@ -28,6 +29,9 @@ int main() {
         const long long got = f2ll_rn(x);
         checked++;
         if (want != got) { if (bad++ < 5) std::printf("f2ll %a want %lld got %lld\n", x, want, got); }
+        const long long got_b = f2ll_rn_bounded(x);
+        checked++;
+        if (want != got_b) { if (bad++ < 5) std::printf("f2ll_bounded %a want %lld got %lld\n", x, want, got_b); }
     };
     auto check_l = [&](long long v) {
         const float want = (float)v;
@@ -36,7 +40,10 @@ int main() {
         if (std::memcmp(&want, &got, 4) != 0) { if (bad++ < 5) std::printf("ll2f %lld want %a got %a\n", v, want, got); }
     };
     const float edges[] = {0.0f, -0.0f, 0.5f, -0.5f, 1.5f, 2.5f, -2.5f, 0.49999997f, 1e-40f, -1e-40f,
-                           8388607.5f, 8388608.0f, 16777215.0f, 16777217.0f, 4.6e18f, -4.6e18f, 9.2e18f};
+                           8388607.5f, 8388608.0f, 16777215.0f, 16777217.0f, 4.6e18f, -4.6e18f, 9.2e18f,
+                           2147483520.0f, 2147483648.0f, -2147483648.0f, -2147483904.0f, 4294967296.0f,
+                           -4294967296.0f, 4294967040.0f, -4294967040.0f, 1.5e10f, -1.5e10f, 4.611686e18f,
+                           -4.611686e18f, 4.6116855e18f, -4.6116855e18f};
     for (float x : edges) check_f(x);
     for (int i = 0; i < 4000000; i++) {
         unsigned u = (unsigned)rng();
