@@ -165,8 +165,10 @@ __device__ __forceinline__ void fir_store(const float2 ys[4], int64_t line, int 
 }
 
 // One work item per CTA: line blockIdx.y, outputs blockIdx.x * blockDim.x * 4 ...
+// (at most 102 registers: 96 in the complex-bin kernel, so that an SM holds 20
+// warps -- six 96-thread CTAs, their shared memory permitting -- not 16)
 template <bool PD, bool TAPS_SMEM>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
     convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
                                const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
                                int tap_start, int64_t M, int center, int D, int nd, int sub, int row, int cols,
