@@ -770,6 +770,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
 // Scatterers per staged chunk of the per-pair kernel (lines per CTA:
 // PAIR_THREADS in kernels.hpp).
 constexpr int PAIR_CHUNK = 256;
+// Control points staged per scatterer at the full chunk size (a cubic spline's
+// tile window: 4 plus one per extra knot interval); wider windows stage fewer
+// scatterers per chunk.  30 KB of shared memory per CTA: seven fit an SM.
+constexpr int PAIR_SPAN = 6;
 
 // Exact arc-projection time of flight of one pair in float-pair arithmetic (fp64 mode).
 // (dx, dy, dz): the scatterer relative to the line origin as pairs.  Returns
@@ -829,7 +833,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     // control points relative to its first one (R, in sr), the global index for
     // the exact re-evaluation at rounding ties; splines (reference mode) the
     // control points themselves
-    __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? MAX_SPLINE_DEGREE + 1 : 1)];
+    __shared__ float4 sp[PAIR_CHUNK * (SPLINE ? PAIR_SPAN : 1)];
     __shared__ float sa[PAIR_CHUNK];
     __shared__ float4 sr[SPLINE && !REF ? PAIR_CHUNK : 1];
     __shared__ int sidx[SPLINE && !REF ? PAIR_CHUNK : 1];
@@ -845,7 +849,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     // control points staged per scatterer, and scatterers per chunk so that
     // they fit the shared array
     const int span = SPLINE ? tile.span : 1;
-    const int chunk = SPLINE ? min(PAIR_CHUNK, PAIR_CHUNK * (MAX_SPLINE_DEGREE + 1) / span) : PAIR_CHUNK;
+    const int chunk = SPLINE ? min(PAIR_CHUNK, PAIR_CHUNK * PAIR_SPAN / span) : PAIR_CHUNK;
     const bool active = tid < tile.count;
     const int line = __ldg(line_ids + tile.first + (active ? tid : 0));
     const LineGeom* g = lines + line;
