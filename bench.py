@@ -12,9 +12,12 @@ convolution, demodulation, decimation).  Prints one JSON line on rank 0.
 * value: projections/s with the phantom resident on the device, IQ left on the
   device, CUDA events around each step on the simulator's stream, L2 flushed
   (a 512 MiB memset) between steps outside the timed events.
-* e2e: the same metric through the C ABI with host buffers: every step uploads
-  the scatterers from pinned host memory (bcsim_set_fixed_scatterers) and reads
-  the IQ back (bcsim_simulate_lines), host wall clock.
+* e2e: the same metric through the C ABI with host buffers, host wall clock:
+  every step (frame) uploads the scatterers from pinned host memory and reads
+  the IQ back.  A fixed-scatterer phantom runs as a stream of frames through
+  bcsim_simulate_fixed_frames (frame k+1's upload overlaps frame k); splines
+  per step (bcsim_set_*_scatterers + bcsim_simulate_lines).  e2e.single_frame
+  is the per-step form for every workload.
 * roofline: the projection kernel against the FP32 pipe: the per-projection
   flop count (flops_per_projection) times the pairs the kernel visits (counted
   by one instrumented run outside the timed region; the exact slot masks skip
@@ -266,11 +269,26 @@ def run_gpu(args):
         t0 = time.perf_counter()
         e2e_step()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_total = sum(e2e_ms) / 1e3
+    e2e_single = sum(e2e_ms) / 1e3
+    # a stream of frames of a fixed-scatterer phantom through one C-ABI call
+    # (bcsim_simulate_fixed_frames): every frame is uploaded and its IQ read back,
+    # frame k+1's upload overlapping frame k's simulation.  One frame's working
+    # set (0.55 GB of bins here) exceeds L2, so no flush between frames.
+    frames_mode = len(host_in) == 1 and not host_sp
+    e2e_total = e2e_single
+    if frames_mode:
+        outs = [torch.empty((L, nd), dtype=torch.complex64, pin_memory=True).numpy() for _ in range(args.steps)]
+        W = max(1, min(args.warmup, args.steps))
+        sim.simulate_fixed_frames([host_in[0]] * W, outs[:W])
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.simulate_fixed_frames([host_in[0]] * args.steps, outs)
+        e2e_total = time.perf_counter() - t0
     if world > 1:
-        t = torch.tensor([e2e_total], device="cuda")
+        t = torch.tensor([e2e_total, e2e_single], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+        e2e_total, e2e_single = float(t[0].item()), float(t[1].item())
     h2d = sum(h.nbytes for h in host_in) + sum(kn.nbytes + cp.nbytes + am.nbytes for _, kn, cp, am in host_sp)
     d2h = L * nd * 8
 
@@ -331,7 +349,13 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": projections * args.steps * world / e2e_total, "unit": "projections/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": e2e_total * 1e3 / args.steps},
+                "ms_per_step": e2e_total * 1e3 / args.steps,
+                "mode": ("frames: one bcsim_simulate_fixed_frames call of `steps` frames from pinned host memory, "
+                         "frame k+1 uploaded while frame k is simulated") if frames_mode else
+                        "per step: clear + add scatterers (upload), simulate_lines (IQ to pinned host memory)",
+                "single_frame": {"value": projections * args.steps * world / e2e_single,
+                                 "ms_per_step": e2e_single * 1e3 / args.steps,
+                                 "mode": "per step: clear + add scatterers (upload), simulate_lines, L2 flushed"}},
         "roofline": {"bound": "fp32", "kernel": "project_shared_kernel" if shared_path else "project_generic_kernel",
                      "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved_tflops / fp32_peak, "traffic": traffic,

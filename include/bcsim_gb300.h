@@ -122,6 +122,19 @@ int bcsim_get_output_shape(const bcsim_handle* h, int64_t* num_lines, int64_t* n
 int bcsim_simulate_lines(bcsim_handle* h, float* out, int64_t cap_complex,
                          int64_t* num_lines, int64_t* num_samples);
 
+/* A stream of frames of fixed scatterers (beside IAlgorithm: the reference's
+ * per-frame clear_fixed_scatterers + add_fixed_scatterers + simulate_lines,
+ * LibBCSim.hpp:57-60,81, in one call).  Frame k, xyza_frames[k] (float [n][4]),
+ * replaces the fixed datasets and is simulated into iq_out_frames[k] (host,
+ * cap_complex complex64 values, [num_lines][num_samples]) -- bit for bit what
+ * those three calls per frame give.  Frame k+1 is uploaded (and its amplitude
+ * bound reduced) on a stream of its own while frame k is simulated; pinned host
+ * frames let the copies overlap.  Blocks until every frame's IQ is on the host;
+ * the last frame stays the fixed dataset.  An error stops at the failing frame
+ * (which then is the fixed dataset). */
+int bcsim_simulate_fixed_frames(bcsim_handle* h, const float* const* xyza_frames, int64_t n, int num_frames,
+                                float* const* iq_out_frames, int64_t cap_complex);
+
 /* simulate_lines into a device buffer (complex64 [num_lines][num_samples], at
  * least 16-byte aligned) on the handle's stream, without a host copy and
  * without synchronising.  For callers that keep the IQ on the GPU. */

@@ -165,6 +165,30 @@ class RfSimulator:
                                                    C.byref(L), C.byref(nd)))
         return out
 
+    def simulate_fixed_frames(self, frames, outs=None):
+        """A stream of fixed-scatterer frames (each [n, 4] float32, the same n),
+        each replacing the fixed datasets: returns (or fills) one IQ array
+        [num_lines, num_samples] complex64 per frame, bit for bit what
+        clear_fixed_scatterers + add_fixed_scatterers + simulate_lines_line_major
+        per frame give.  The next frame's upload overlaps the current frame's
+        simulation (pinned host arrays let the copies run asynchronously)."""
+        frames = [_f32(f, "frames must be [n, 4] float32 arrays", 2, 4) for f in frames]
+        if not frames:
+            return []
+        n = frames[0].shape[0]
+        if any(f.shape[0] != n for f in frames):
+            raise ValueError("every frame must hold the same number of scatterers")
+        L, nd = self.output_shape()
+        if outs is None:
+            outs = [np.empty((L, nd), np.complex64) for _ in frames]
+        if len(outs) != len(frames) or any(o.shape != (L, nd) or o.dtype != np.complex64 or
+                                           not o.flags.c_contiguous for o in outs):
+            raise ValueError("outs must hold one C-contiguous complex64 [num_lines, num_samples] array per frame")
+        fp = (C.POINTER(C.c_float) * len(frames))(*[f.ctypes.data_as(C.POINTER(C.c_float)) for f in frames])
+        op = (C.POINTER(C.c_float) * len(outs))(*[o.ctypes.data_as(C.POINTER(C.c_float)) for o in outs])
+        self._check(self._lib.bcsim_simulate_fixed_frames(self._h, fp, n, len(frames), op, L * nd))
+        return outs
+
     def simulate_lines_device(self, device_ptr: int, capacity: int):
         """IQ into a device buffer of `capacity` complex64 values (no host copy)."""
         self._check(self._lib.bcsim_simulate_lines_device(self._h, C.c_void_p(device_ptr), int(capacity)))

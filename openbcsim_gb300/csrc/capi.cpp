@@ -166,6 +166,11 @@ int bcsim_simulate_lines(bcsim_handle* h, float* out, int64_t cap_complex, int64
     return guarded(h, [&] { h->sim.simulate_host(out, cap_complex, num_lines, num_samples); });
 }
 
+int bcsim_simulate_fixed_frames(bcsim_handle* h, const float* const* xyza_frames, int64_t n, int num_frames,
+                                float* const* iq_out_frames, int64_t cap_complex) {
+    return guarded(h, [&] { h->sim.simulate_fixed_frames(xyza_frames, n, num_frames, iq_out_frames, cap_complex); });
+}
+
 int bcsim_simulate_lines_device(bcsim_handle* h, void* device_out, int64_t cap_complex) {
     return guarded(h, [&] { h->sim.simulate_device(device_out, cap_complex); });
 }

@@ -105,6 +105,11 @@ void Simulator::ensure_device() {
     BCSIM_CUDA(cudaStreamCreateWithFlags(&owned_stream_.s, cudaStreamNonBlocking));
     BCSIM_CUDA(cudaStreamCreateWithFlags(&side_stream_.s, cudaStreamNonBlocking));
     BCSIM_CUDA(cudaStreamCreateWithFlags(&copy_stream_.s, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&upload_stream_.s, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; k++) {
+        BCSIM_CUDA(cudaEventCreateWithFlags(&ev_uploaded_[k].e, cudaEventDisableTiming));
+        BCSIM_CUDA(cudaEventCreateWithFlags(&ev_consumed_[k].e, cudaEventDisableTiming));
+    }
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_fork_.e, cudaEventDisableTiming));
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_join_.e, cudaEventDisableTiming));
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_copied_.e, cudaEventDisableTiming));
@@ -376,6 +381,7 @@ void Simulator::set_lookup_profile(const float* samples, int nr, int nl, int ne,
 }
 
 void Simulator::clear_fixed_scatterers() {
+    fixed_src_ = nullptr;
     cfg_version_++;
     data_version_++;
     fixed_n_ = 0;
@@ -1193,7 +1199,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
             const float* origin = lines_[0].o;
             if (fixed_n_ > 0)
                 ++launches;
-                BCSIM_CUDA(launch_prep_shared(fixed_xyza_.as<float4>(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
+                BCSIM_CUDA(launch_prep_shared(fixed_src(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
                                               vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
             for (size_t d = 0; d < splines_.size(); d++) {
                 if (!P.spline_shared[d]) continue;
@@ -1227,7 +1233,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         for (const GenLaunch& g : P.gl) {
             if (g.kind == 0) {
                 ++launches;
-                BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0,
+                BCSIM_CUDA(launch_project_generic(fixed_src(), nullptr, nullptr, fixed_n_, 0, 0,
                                                   vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
                                                   (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
@@ -1253,7 +1259,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         if (g.kind == 0) {
             if (P.shared) continue;
             ++launches;
-                BCSIM_CUDA(launch_project_generic(fixed_xyza_.as<float4>(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
+                BCSIM_CUDA(launch_project_generic(fixed_src(), nullptr, nullptr, fixed_n_, 0, 0, nullptr,
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
                                               b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
@@ -1416,6 +1422,72 @@ void Simulator::simulate_host(float* host_out, int64_t cap_complex, int64_t* lin
     ensure_device();
     out_.reserve((size_t)L * nd * sizeof(float2), stream_);
     simulate(out_.as<float2>(), host_out);
+}
+
+void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int num_frames, float* const* outs,
+                                      int64_t cap_complex) {
+    if (num_frames <= 0) return;
+    if (n <= 0 || !frames || !outs) throw SimError(BCSIM_E_INVALID, "simulate_fixed_frames: invalid data");
+    for (int k = 0; k < num_frames; k++)
+        if (!frames[k] || !outs[k]) throw SimError(BCSIM_E_INVALID, "simulate_fixed_frames: null frame or output");
+    ensure_device();
+    int64_t L = 0, nd = 0;
+    output_shape(&L, &nd);
+    if (cap_complex < L * nd)
+        throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
+    const size_t bytes = (size_t)n * sizeof(float4);
+    for (int b = 0; b < 2; b++) {
+        frame_xyza_[b].reserve(bytes, stream_);
+        frame_scratch_[b].reserve(abs_sum_scratch_bytes(), stream_);
+    }
+    if (!frame_bounds_.p) BCSIM_CUDA(cudaMallocHost(&frame_bounds_.p, sizeof(FrameBounds)));
+    out_.reserve((size_t)L * nd * sizeof(float2), stream_);
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));   // the buffers exist before the upload stream uses them
+    const cudaStream_t up = upload_stream_.s;
+    // frame k: into buffer k & 1, once the frame that read it last (k - 2) is done
+    auto upload = [&](int k) {
+        const int b = k & 1;
+        if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(up, ev_consumed_[b].e, 0));
+        BCSIM_CUDA(cudaMemcpyAsync(frame_xyza_[b].get(), frames[k], bytes, cudaMemcpyHostToDevice, up));
+        BCSIM_CUDA(abs_sum_enqueue(frame_xyza_[b].as<float>() + 3, 4, n, frame_scratch_[b].get(),
+                                   &frame_bounds_.p->sum[b], &frame_bounds_.p->nonfinite[b], up));
+        BCSIM_CUDA(cudaEventRecord(ev_uploaded_[b].e, up));
+    };
+    // afterwards (or on an error) the frame last installed is the fixed dataset
+    int installed = -1;
+    auto settle = [&]() {
+        cudaStreamSynchronize(up);
+        cudaStreamSynchronize(stream_);
+        if (installed >= 0) std::swap(fixed_xyza_, frame_xyza_[installed & 1]);
+        fixed_src_ = nullptr;
+    };
+    try {
+        upload(0);
+        for (int k = 0; k < num_frames; k++) {
+            const int b = k & 1;
+            if (k + 1 < num_frames) upload(k + 1);
+            BCSIM_CUDA(cudaEventSynchronize(ev_uploaded_[b].e));   // frame k's amplitude bound
+            fixed_src_ = frame_xyza_[b].as<float4>();
+            installed = k;
+            fixed_n_ = n;
+            num_fixed_sets_ = 1;
+            fixed_sum_abs_ = frame_bounds_.p->sum[b];
+            amplitude_nonfinite_ = frame_bounds_.p->nonfinite[b] != 0;
+            cfg_version_++;
+            data_version_++;
+            prepare();   // a new frame of the same shape: the scale and the records' identity
+            BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_uploaded_[b].e, 0));
+            enqueue(stream_, out_.as<float2>(), false, outs[k]);
+            BCSIM_CUDA(cudaEventRecord(ev_consumed_[b].e, stream_));
+        }
+        if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
+        BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, stream_));
+    } catch (...) {
+        settle();
+        throw;
+    }
+    settle();
+    if (*flag_host_.p) check_device_flag();
 }
 
 void Simulator::simulate_device(void* dev_out, int64_t cap_complex) {

@@ -54,6 +54,21 @@ private:
     cudaStream_t stream_ = nullptr;   // stream-ordered allocation on this stream (null: cudaMalloc)
 };
 
+// Pinned host landing places of the two in-flight frames' amplitude bounds.
+struct FrameBounds {
+    double sum[2];
+    int nonfinite[2];
+};
+struct PinnedFrameBounds {
+    FrameBounds* p = nullptr;
+    PinnedFrameBounds() = default;
+    PinnedFrameBounds(const PinnedFrameBounds&) = delete;
+    PinnedFrameBounds& operator=(const PinnedFrameBounds&) = delete;
+    ~PinnedFrameBounds() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 // Pinned host int (the error flag's landing place), freed with its owner.
 struct PinnedInt {
     int* p = nullptr;
@@ -187,6 +202,14 @@ public:
     // frame k with every line's timestamp advanced by k * prt, into device
     // memory [P][L][nd].  The scan sequence is restored afterwards.
     void simulate_packet(int P, float prt, float2* dev_out, int64_t cap_complex);
+    // A stream of frames of fixed scatterers: frame k (n scatterers, host
+    // float4 xyza, replacing the fixed datasets) simulated into host IQ outs[k]
+    // (cap_complex values each), as clear + add_fixed_scatterers +
+    // simulate_lines per frame would, bit for bit.  Frame k+1's upload and
+    // amplitude bound run on their own stream while frame k is simulated.
+    // Afterwards the last frame is the fixed dataset.
+    void simulate_fixed_frames(const float* const* frames, int64_t n, int num_frames, float* const* outs,
+                               int64_t cap_complex);
 
     std::vector<double> get_debug_data(const std::string& key) const;
     void set_logger(LogFn fn, void* user) { log_fn_ = fn; log_user_ = user; }
@@ -203,6 +226,7 @@ private:
     void set_fixed_point_scale(SimParams& p) const;
     uint64_t records_key_of(const Plan& P) const;
     std::vector<double> data_shape() const;
+    const float4* fixed_src() const { return fixed_src_ ? fixed_src_ : fixed_xyza_.as<float4>(); }
 
     // configuration
     int device_ = 0;
@@ -210,7 +234,9 @@ private:
     OwnedStream owned_stream_;
     OwnedStream side_stream_;   // bins cleared here while the records are prepared
     OwnedStream copy_stream_;   // IQ copied to the host here while later lines are convolved
+    OwnedStream upload_stream_;   // simulate_fixed_frames: the next frame's upload
     OwnedEvent ev_fork_, ev_join_, ev_copied_;
+    OwnedEvent ev_uploaded_[2], ev_consumed_[2];   // per frame buffer: upload done / last reader done
     std::vector<cudaEvent_t> ev_blocks_;   // one per convolution block (owned, see ~Simulator)
     PinnedInt flag_host_;
     cudaStream_t stream_ = nullptr;   // owned_stream_.s
@@ -269,6 +295,9 @@ private:
 
     // all fixed datasets, appended into one float4 [n] array (x, y, z, a)
     DeviceBuffer fixed_xyza_;
+    DeviceBuffer frame_xyza_[2], frame_scratch_[2];   // simulate_fixed_frames' double buffer
+    PinnedFrameBounds frame_bounds_;
+    const float4* fixed_src_ = nullptr;   // the fixed scatterers the kernels read: fixed_xyza_ unless a frame's
     int64_t fixed_n_ = 0;
     int num_fixed_sets_ = 0;
     double fixed_sum_abs_ = 0.0;

@@ -75,21 +75,29 @@ cudaError_t launch_spline_transpose(const float* raw, int64_t n, int num_cs, flo
 
 size_t abs_sum_scratch_bytes() { return (SUM_BLOCKS + 1) * sizeof(double) + sizeof(int); }
 
+cudaError_t abs_sum_enqueue(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
+                            cudaStream_t stream) {
+    double* partial = static_cast<double*>(scratch);
+    double* out = partial + SUM_BLOCKS;
+    int* bad = reinterpret_cast<int*>(out + 1);
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) + sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    if (n > 0) {
+        abs_sum_partial_kernel<<<SUM_BLOCKS, SUM_THREADS, 0, stream>>>(vals, stride, n, partial, bad);
+        abs_sum_final_kernel<<<1, SUM_THREADS, 0, stream>>>(partial, SUM_BLOCKS, out);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = cudaMemcpyAsync(sum, out, sizeof(double), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
+    return cudaMemcpyAsync(nonfinite, bad, sizeof(int), cudaMemcpyDeviceToHost, stream);
+}
+
 cudaError_t abs_sum(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
                     cudaStream_t stream) {
     *sum = 0.0;
     *nonfinite = 0;
     if (n <= 0) return cudaSuccess;
-    double* partial = static_cast<double*>(scratch);
-    double* out = partial + SUM_BLOCKS;
-    int* bad = reinterpret_cast<int*>(out + 1);
-    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), stream);
+    cudaError_t e = abs_sum_enqueue(vals, stride, n, scratch, sum, nonfinite, stream);
     if (e != cudaSuccess) return e;
-    abs_sum_partial_kernel<<<SUM_BLOCKS, SUM_THREADS, 0, stream>>>(vals, stride, n, partial, bad);
-    abs_sum_final_kernel<<<1, SUM_THREADS, 0, stream>>>(partial, SUM_BLOCKS, out);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(sum, out, sizeof(double), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
-    if ((e = cudaMemcpyAsync(nonfinite, bad, sizeof(int), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
     return cudaStreamSynchronize(stream);
 }
 

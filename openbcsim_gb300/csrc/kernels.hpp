@@ -220,6 +220,10 @@ cudaError_t launch_spline_transpose(const float* raw, int64_t n, int num_cs, flo
 size_t abs_sum_scratch_bytes();
 cudaError_t abs_sum(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
                     cudaStream_t stream);
+// The same without synchronising: *sum and *nonfinite (pinned host memory) are
+// written in stream order.
+cudaError_t abs_sum_enqueue(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
+                            cudaStream_t stream);
 
 cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream);
 // Copy of the error flag into host memory (pinned: asynchronous), in stream order.
