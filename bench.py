@@ -272,9 +272,13 @@ def run_gpu(args):
     e2e_single = sum(e2e_ms) / 1e3
     # a stream of frames of a fixed-scatterer phantom through one C-ABI call
     # (bcsim_simulate_fixed_frames): every frame is uploaded and its IQ read back,
-    # frame k+1's upload overlapping frame k's simulation.  One frame's working
-    # set (0.55 GB of bins here) exceeds L2, so no flush between frames.
-    frames_mode = len(host_in) == 1 and not host_sp
+    # frame k+1's upload overlapping frame k's simulation.  No L2 flush fits
+    # between the frames of one call, so this form is used only where one
+    # frame's bins alone exceed L2 (0.55 GB on the 3-D volume; smaller
+    # workloads keep the per-step form, flushed)
+    bins_bytes = L * job.num_samples * (16 if job.phase_delay else 8)
+    l2_bytes = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", 0) or (129 << 20)
+    frames_mode = len(host_in) == 1 and not host_sp and bins_bytes > 2 * l2_bytes
     e2e_total = e2e_single
     if frames_mode:
         outs = [torch.empty((L, nd), dtype=torch.complex64, pin_memory=True).numpy() for _ in range(args.steps)]
@@ -351,8 +355,8 @@ def run_gpu(args):
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_total * 1e3 / args.steps,
                 "mode": ("frames: one bcsim_simulate_fixed_frames call of `steps` frames from pinned host memory, "
-                         "frame k+1 uploaded while frame k is simulated") if frames_mode else
-                        "per step: clear + add scatterers (upload), simulate_lines (IQ to pinned host memory)",
+                         "frame k+1 uploaded while frame k is simulated; one frame's bins exceed L2") if frames_mode else
+                        "per step: clear + add scatterers (upload), simulate_lines (IQ to pinned host memory), L2 flushed",
                 "single_frame": {"value": projections * args.steps * world / e2e_single,
                                  "ms_per_step": e2e_single * 1e3 / args.steps,
                                  "mode": "per step: clear + add scatterers (upload), simulate_lines, L2 flushed"}},
