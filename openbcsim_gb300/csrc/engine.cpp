@@ -109,6 +109,7 @@ void Simulator::ensure_device() {
     for (int k = 0; k < 2; k++) {
         BCSIM_CUDA(cudaEventCreateWithFlags(&ev_uploaded_[k].e, cudaEventDisableTiming));
         BCSIM_CUDA(cudaEventCreateWithFlags(&ev_consumed_[k].e, cudaEventDisableTiming));
+        BCSIM_CUDA(cudaEventCreateWithFlags(&ev_out_free_[k].e, cudaEventDisableTiming));
     }
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_fork_.e, cudaEventDisableTiming));
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_join_.e, cudaEventDisableTiming));
@@ -1157,7 +1158,7 @@ void Simulator::prepare() {
 // ---------------------------------------------------------------------------
 // enqueue: device work only (capturable: no allocation, no host copy, no sync)
 // ---------------------------------------------------------------------------
-void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out) {
+void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out, bool wait_copies) {
     const Plan& P = plan_;
     const SimParams& p = P.p;
     const BeamDev& b = P.b;
@@ -1316,7 +1317,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     }
     if (host_out) {
         BCSIM_CUDA(cudaEventRecord(ev_copied_.e, copy_stream_.s));
-        BCSIM_CUDA(cudaStreamWaitEvent(st, ev_copied_.e, 0));
+        if (wait_copies) BCSIM_CUDA(cudaStreamWaitEvent(st, ev_copied_.e, 0));
     }
     if (timing) {
         debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
@@ -1439,9 +1440,9 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
     for (int b = 0; b < 2; b++) {
         frame_xyza_[b].reserve(bytes, stream_);
         frame_scratch_[b].reserve(abs_sum_scratch_bytes(), stream_);
+        frame_out_[b].reserve((size_t)L * nd * sizeof(float2), stream_);
     }
     if (!frame_bounds_.p) BCSIM_CUDA(cudaMallocHost(&frame_bounds_.p, sizeof(FrameBounds)));
-    out_.reserve((size_t)L * nd * sizeof(float2), stream_);
     BCSIM_CUDA(cudaStreamSynchronize(stream_));   // the buffers exist before the upload stream uses them
     const cudaStream_t up = upload_stream_.s;
     // frame k: into buffer k & 1, once the frame that read it last (k - 2) is done
@@ -1457,6 +1458,7 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
     int installed = -1;
     auto settle = [&]() {
         cudaStreamSynchronize(up);
+        cudaStreamSynchronize(copy_stream_.s);
         cudaStreamSynchronize(stream_);
         if (installed >= 0) std::swap(fixed_xyza_, frame_xyza_[installed & 1]);
         fixed_src_ = nullptr;
@@ -1477,9 +1479,14 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
             data_version_++;
             prepare();   // a new frame of the same shape: the scale and the records' identity
             BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_uploaded_[b].e, 0));
-            enqueue(stream_, out_.as<float2>(), false, outs[k]);
+            // two device outputs too: frame k + 1 is convolved while frame k's
+            // last block is still copied to the host
+            if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_out_free_[b].e, 0));
+            enqueue(stream_, frame_out_[b].as<float2>(), false, outs[k], false);
             BCSIM_CUDA(cudaEventRecord(ev_consumed_[b].e, stream_));
+            BCSIM_CUDA(cudaEventRecord(ev_out_free_[b].e, copy_stream_.s));
         }
+        BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_copied_.e, 0));   // the last frame's copies
         if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
         BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, stream_));
     } catch (...) {

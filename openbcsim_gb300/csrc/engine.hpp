@@ -180,8 +180,8 @@ public:
     // prepare()).  With host_out (pinned or pageable host memory), the
     // convolution runs in blocks of lines and each block's IQ is copied to
     // host_out on a copy stream while the next block is convolved; st then
-    // waits for the copies.
-    void enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out = nullptr);
+    // waits for the copies unless wait_copies is false (ev_copied_ marks them).
+    void enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out = nullptr, bool wait_copies = true);
     // Copy the whole configuration of o (parameters, excitation, beam, scatterer
     // datasets -- device copies; not the scan sequence) into this simulator.
     void clone_from(Simulator& o);
@@ -295,7 +295,8 @@ private:
 
     // all fixed datasets, appended into one float4 [n] array (x, y, z, a)
     DeviceBuffer fixed_xyza_;
-    DeviceBuffer frame_xyza_[2], frame_scratch_[2];   // simulate_fixed_frames' double buffer
+    DeviceBuffer frame_xyza_[2], frame_scratch_[2], frame_out_[2];   // simulate_fixed_frames' double buffers
+    OwnedEvent ev_out_free_[2];   // a frame output buffer's copy to the host done
     PinnedFrameBounds frame_bounds_;
     const float4* fixed_src_ = nullptr;   // the fixed scatterers the kernels read: fixed_xyza_ unless a frame's
     int64_t fixed_n_ = 0;
