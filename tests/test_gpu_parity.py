@@ -238,6 +238,31 @@ def test_full_size_lines_vs_oracle(oracle, which):
         assert oracle.rel_rms(iq[lo:lo + 4], ref) <= FP64_TOL, (which, lo)
 
 
+def test_large_phantom_few_lines(oracle):
+    """30 million fixed scatterers (0.5 GB of phantom, 1 GB of sorted records)
+    on 8 lines of the 3-D LUT volume: every record chunk, sort key and count
+    stays in range; the IQ matches the FP64 oracle."""
+    from openbcsim_gb300 import workloads as W
+
+    job = W.volume_3d_lut(num_scatterers=30_000_000, n_az=4, n_el=2)
+    iq = run(job)
+    assert np.isfinite(iq).all()
+    assert oracle.rel_rms(iq, oracle.simulate(job, oracle.MODE_FP64)) <= FP64_TOL
+
+
+def test_many_lines(oracle):
+    """128 x 128 = 16384 lines (sixteen 1024-line groups per record chunk):
+    lines from the first, a middle and the last group match the FP64 oracle."""
+    from openbcsim_gb300 import workloads as W
+
+    job = W.volume_3d_lut(num_scatterers=200_000, n_az=128, n_el=128)
+    iq = run(job)
+    assert iq.shape[0] == 16384 and np.isfinite(iq).all()
+    for lo in (0, 8190, 16380):
+        ref = oracle.simulate(job, oracle.MODE_FP64, line_begin=lo, line_end=lo + 4)
+        assert oracle.rel_rms(iq[lo:lo + 4], ref) <= FP64_TOL, lo
+
+
 @pytest.mark.parametrize("name", ["sector_pd", "sector_nopd", "lut3d", "edge", "spline", "linear"])
 def test_culling_is_exact(name):
     """Skipping (scatterer, line-slot) pairs whose weight is provably zero
