@@ -32,12 +32,14 @@
 //      the demodulation factor for the n' = m D / F.
 //
 // Shared memory holds the array padded by one float2 per 16 (element i at
-// i + i/16): every pass then reads and writes without bank conflicts (two
-// wavefronts per warp access of 8 bytes).  It also holds a quarter-wave table
-// of twiddles W_M^y, y < M/4, copied from a host-made table (double precision
-// rounded once); a task reads four of them and multiplies out the rest.  M =
-// 8192 then takes 87 KB, two CTAs per SM; M = 16384 one.  FP32 throughout:
-// the relative RMS error is ~2e-7 of the IQ.
+// i + i/16): every pass then reads and writes its data without bank conflicts
+// (two wavefronts per warp access of 8 bytes).  It also holds a quarter-wave
+// table of twiddles W_M^y, y < M/4, copied from a host-made table (double
+// precision rounded once); a task reads four of them (at strided exponents,
+// so these reads do conflict) and multiplies out the rest; the first pass
+// reads its four from the host-made table while the copy proceeds.  M = 8192
+// then takes 87 KB, two CTAs per SM; M = 16384 one.  FP32 throughout: the
+// relative RMS error is ~2e-7 of the IQ.
 #include <cmath>
 #include <complex>
 #include <cstdint>
