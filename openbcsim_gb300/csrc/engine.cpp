@@ -106,7 +106,9 @@ void Simulator::ensure_device() {
     BCSIM_CUDA(cudaStreamCreateWithFlags(&side_stream_.s, cudaStreamNonBlocking));
     BCSIM_CUDA(cudaStreamCreateWithFlags(&copy_stream_.s, cudaStreamNonBlocking));
     BCSIM_CUDA(cudaStreamCreateWithFlags(&upload_stream_.s, cudaStreamNonBlocking));
+    BCSIM_CUDA(cudaStreamCreateWithFlags(&prep_stream_.s, cudaStreamNonBlocking));
     for (int k = 0; k < 2; k++) {
+        BCSIM_CUDA(cudaEventCreateWithFlags(&ev_staged_[k].e, cudaEventDisableTiming));
         BCSIM_CUDA(cudaEventCreateWithFlags(&ev_uploaded_[k].e, cudaEventDisableTiming));
         BCSIM_CUDA(cudaEventCreateWithFlags(&ev_consumed_[k].e, cudaEventDisableTiming));
         BCSIM_CUDA(cudaEventCreateWithFlags(&ev_out_free_[k].e, cudaEventDisableTiming));
@@ -1095,20 +1097,13 @@ void Simulator::prepare() {
     // device buffers
     const int stride = phase_delay_ ? 2 : 1;
     P.bins_bytes = (size_t)L * ns * stride * sizeof(unsigned long long);
-    bins_.reserve(P.bins_bytes, stream_);
-    counts_.reserve(4 * sizeof(int), stream_);
+    bins_[cur_].reserve(P.bins_bytes, stream_);
+    rec().counts.reserve(4 * sizeof(int), stream_);
     pair_counts_.reserve(4 * sizeof(unsigned long long), stream_);
     out_.reserve((size_t)L * nd_ * sizeof(float2), stream_);
     P.spline_off.assign(splines_.size(), -1);
     if (P.n_shared > 0) {
         const int64_t N = P.n_shared;
-        keys_in_.reserve(N * sizeof(uint32_t), stream_);
-        vals_in_.reserve(N * sizeof(uint32_t), stream_);
-        keys_out_.reserve(N * sizeof(uint32_t), stream_);
-        vals_out_.reserve(N * sizeof(uint32_t), stream_);
-        recA_.reserve(N * sizeof(float4), stream_);
-        recB_.reserve(N * sizeof(float4), stream_);
-        records_.reserve((size_t)N * 2 * sizeof(float4), stream_);
         int64_t off = fixed_n_;
         std::vector<double> bd(64 * std::max<size_t>(1, splines_.size()), 0.0);
         std::vector<float> bf(64 * std::max<size_t>(1, splines_.size()), 0.0f);
@@ -1133,11 +1128,7 @@ void Simulator::prepare() {
         int end_bit = 1;
         while ((1ll << end_bit) < (int64_t)ns + 2) end_bit++;
         P.end_bit = end_bit;
-        size_t tmp_bytes = 0;
-        BCSIM_CUDA(radix_sort_pairs(nullptr, &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
-                                    vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, end_bit, st));
-        sort_tmp_.reserve(tmp_bytes, stream_);
-        P.sort_tmp_bytes = tmp_bytes;
+        reserve_records(rec(), P);
         // records per CTA: enough CTAs to fill the GPU several times over, a
         // multiple of the fold group (512 records when chunks of 512 fill the
         // GPU, else 128), so that results do not depend on the chunk
@@ -1155,10 +1146,67 @@ void Simulator::prepare() {
     if (autotune_) autotune();
 }
 
+// Buffers of one record set for plan P (P.end_bit set; fills P.sort_tmp_bytes).
+void Simulator::reserve_records(RecordSet& R, Plan& P) {
+    R.counts.reserve(4 * sizeof(int), stream_);
+    const int64_t N = P.n_shared;
+    if (N <= 0) return;
+    R.keys_in.reserve(N * sizeof(uint32_t), stream_);
+    R.vals_in.reserve(N * sizeof(uint32_t), stream_);
+    R.keys_out.reserve(N * sizeof(uint32_t), stream_);
+    R.vals_out.reserve(N * sizeof(uint32_t), stream_);
+    R.recA.reserve(N * sizeof(float4), stream_);
+    R.recB.reserve(N * sizeof(float4), stream_);
+    R.records.reserve((size_t)N * 2 * sizeof(float4), stream_);
+    size_t tmp_bytes = 0;
+    BCSIM_CUDA(radix_sort_pairs(nullptr, &tmp_bytes, R.keys_in.as<uint32_t>(), R.keys_out.as<uint32_t>(),
+                                R.vals_in.as<uint32_t>(), R.vals_out.as<uint32_t>(), N, P.end_bit, stream_));
+    R.sort_tmp.reserve(tmp_bytes, stream_);
+    P.sort_tmp_bytes = tmp_bytes;
+}
+
+// The shared-origin records in bin order (unless the set already holds them):
+// per-scatterer prep, radix sort by bin, bin-range counts, gather.
+void Simulator::enqueue_records(cudaStream_t st, int* launches) {
+    const Plan& P = plan_;
+    RecordSet& R = rec();
+    if (P.n_shared <= 0 || (record_cache_ && R.key == P.records_key)) return;
+    const SimParams& p = P.p;
+    const BeamDev& b = P.b;
+    const int64_t N = P.n_shared;
+    const int ns = (int)ns_;
+    const float* origin = lines_[0].o;
+    if (fixed_n_ > 0) {
+        ++*launches;
+        BCSIM_CUDA(launch_prep_shared(fixed_src(), fixed_n_, 0, origin, p, b, R.keys_in.as<uint32_t>(),
+                                      R.vals_in.as<uint32_t>(), R.recA.as<float4>(), R.recB.as<float4>(), st));
+    }
+    for (size_t d = 0; d < splines_.size(); d++) {
+        if (!P.spline_shared[d]) continue;
+        const SplineDataset& ds = splines_[d];
+        ++*launches;
+        BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                                             P.spline_first_cs[d], ds.degree, spl_basis_d_.as<double>() + 64 * d,
+                                             spl_basis_f_.as<float>() + 64 * d, P.spline_off[d], origin, p, b,
+                                             R.keys_in.as<uint32_t>(), R.vals_in.as<uint32_t>(), R.recA.as<float4>(),
+                                             R.recB.as<float4>(), st));
+    }
+    size_t tmp_bytes = P.sort_tmp_bytes;
+    BCSIM_CUDA(radix_sort_pairs(R.sort_tmp.get(), &tmp_bytes, R.keys_in.as<uint32_t>(), R.keys_out.as<uint32_t>(),
+                                R.vals_in.as<uint32_t>(), R.vals_out.as<uint32_t>(), N, P.end_bit, st));
+    *launches += 3;   // init, count, finish
+    BCSIM_CUDA(launch_count_keys(R.keys_out.as<uint32_t>(), N, ns, R.counts.as<int>(), st));
+    ++*launches;
+    BCSIM_CUDA(launch_gather_records(R.vals_out.as<uint32_t>(), R.counts.as<int>(), N, R.recA.as<float4>(),
+                                     R.recB.as<float4>(), R.records.as<float4>(), N, st));
+    R.key = P.records_key;
+}
+
 // ---------------------------------------------------------------------------
 // enqueue: device work only (capturable: no allocation, no host copy, no sync)
 // ---------------------------------------------------------------------------
-void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out, bool wait_copies) {
+void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out, bool wait_copies,
+                        bool staged) {
     const Plan& P = plan_;
     const SimParams& p = P.p;
     const BeamDev& b = P.b;
@@ -1166,13 +1214,14 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     const int ns = (int)ns_;
     EventTimer total(timing, st);
     EventTimer timer(timing, st);
-    unsigned long long* bins = bins_.as<unsigned long long>();
+    unsigned long long* bins = bins_[cur_].as<unsigned long long>();
+    RecordSet& R = rec();
     int launches = 0;   // kernels of this library launched (the radix sort's are counted apart)
     const LineGeom* lines_d = lines_dev_.as<LineGeom>();
     // the bins are cleared on the side stream, after st's earlier work (the
     // previous convolution read them), while the records are prepared; st
     // waits for it before the first kernel that writes bins
-    {
+    if (!staged) {
         const cudaStream_t side = side_stream_.s;
         EventTimer mt(timing, side);
         BCSIM_CUDA(cudaEventRecord(ev_fork_.e, st));
@@ -1182,7 +1231,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         BCSIM_CUDA(cudaEventRecord(ev_join_.e, side));
         if (timing) debug_["kernel_memset_ms"].push_back(mt.stop());
     }
-    bool joined = false;
+    bool joined = staged;
     auto join_bins = [&]() {
         if (!joined) BCSIM_CUDA(cudaStreamWaitEvent(st, ev_join_.e, 0));
         joined = true;
@@ -1196,38 +1245,13 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     if (P.n_shared > 0) {
         const int64_t N = P.n_shared;
         timer.restart();
-        if (!record_cache_ || records_key_ != P.records_key) {
-            const float* origin = lines_[0].o;
-            if (fixed_n_ > 0)
-                ++launches;
-                BCSIM_CUDA(launch_prep_shared(fixed_src(), fixed_n_, 0, origin, p, b, keys_in_.as<uint32_t>(),
-                                              vals_in_.as<uint32_t>(), recA_.as<float4>(), recB_.as<float4>(), st));
-            for (size_t d = 0; d < splines_.size(); d++) {
-                if (!P.spline_shared[d]) continue;
-                const SplineDataset& ds = splines_[d];
-                ++launches;
-                BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
-                                                     P.spline_first_cs[d], ds.degree, spl_basis_d_.as<double>() + 64 * d,
-                                                     spl_basis_f_.as<float>() + 64 * d, P.spline_off[d], origin, p, b,
-                                                     keys_in_.as<uint32_t>(), vals_in_.as<uint32_t>(),
-                                                     recA_.as<float4>(), recB_.as<float4>(), st));
-            }
-            size_t tmp_bytes = P.sort_tmp_bytes;
-            BCSIM_CUDA(radix_sort_pairs(sort_tmp_.get(), &tmp_bytes, keys_in_.as<uint32_t>(), keys_out_.as<uint32_t>(),
-                                        vals_in_.as<uint32_t>(), vals_out_.as<uint32_t>(), N, P.end_bit, st));
-            launches += 3;   // init, count, finish
-            BCSIM_CUDA(launch_count_keys(keys_out_.as<uint32_t>(), N, ns, counts_.as<int>(), st));
-            ++launches;
-            BCSIM_CUDA(launch_gather_records(vals_out_.as<uint32_t>(), counts_.as<int>(), N, recA_.as<float4>(),
-                                             recB_.as<float4>(), records_.as<float4>(), N, st));
-            records_key_ = P.records_key;
-        }
+        if (!staged) enqueue_records(st, &launches);
         if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
         timer.restart();
 
         join_bins();
         ++launches;
-        BCSIM_CUDA(launch_project_shared(records_.as<float4>(), N, counts_.as<int>(), N, P.chunk, lines_d,
+        BCSIM_CUDA(launch_project_shared(R.records.as<float4>(), N, R.counts.as<int>(), N, P.chunk, lines_d,
                                          line_order_dev_.as<int>(), cones_dev_.as<SlotCone>(), L, p, b, bins,
                                          pair_counts, st));
         // near-origin residue, per pair
@@ -1235,7 +1259,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
             if (g.kind == 0) {
                 ++launches;
                 BCSIM_CUDA(launch_project_generic(fixed_src(), nullptr, nullptr, fixed_n_, 0, 0,
-                                                  vals_out_.as<uint32_t>(), counts_.as<int>(), 0, lines_d,
+                                                  R.vals_out.as<uint32_t>(), R.counts.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
                                                   (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
                                                   pair_counts));
@@ -1243,7 +1267,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                 const SplineDataset& ds = splines_[g.d];
                 ++launches;
                 BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
-                                                  ds.degree, vals_out_.as<uint32_t>(), counts_.as<int>(),
+                                                  ds.degree, R.vals_out.as<uint32_t>(), R.counts.as<int>(),
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                                   gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
@@ -1458,11 +1482,14 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
     int installed = -1;
     auto settle = [&]() {
         cudaStreamSynchronize(up);
+        cudaStreamSynchronize(prep_stream_.s);
         cudaStreamSynchronize(copy_stream_.s);
         cudaStreamSynchronize(stream_);
         if (installed >= 0) std::swap(fixed_xyza_, frame_xyza_[installed & 1]);
         fixed_src_ = nullptr;
     };
+    const cudaStream_t ps = prep_stream_.s;
+    bool sets_ready = false;
     try {
         upload(0);
         for (int k = 0; k < num_frames; k++) {
@@ -1477,12 +1504,29 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
             amplitude_nonfinite_ = frame_bounds_.p->nonfinite[b] != 0;
             cfg_version_++;
             data_version_++;
+            cur_ = b;   // bins and record set b
             prepare();   // a new frame of the same shape: the scale and the records' identity
-            BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_uploaded_[b].e, 0));
+            if (!sets_ready) {
+                for (int c = 0; c < 2; c++) {
+                    bins_[c].reserve(plan_.bins_bytes, stream_);
+                    reserve_records(rs_[c], plan_);
+                }
+                BCSIM_CUDA(cudaStreamSynchronize(stream_));   // before the prep stream uses them
+                sets_ready = true;
+            }
+            // frame k's bins cleared and records prepared on the prep stream, once
+            // frame k - 2 (the last user of set b) is done: while frame k - 1 runs
+            BCSIM_CUDA(cudaStreamWaitEvent(ps, ev_uploaded_[b].e, 0));
+            if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(ps, ev_consumed_[b].e, 0));
+            BCSIM_CUDA(cudaMemsetAsync(bins_[b].get(), 0, plan_.bins_bytes, ps));
+            int launches = 0;
+            enqueue_records(ps, &launches);
+            BCSIM_CUDA(cudaEventRecord(ev_staged_[b].e, ps));
+            BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_staged_[b].e, 0));
             // two device outputs too: frame k + 1 is convolved while frame k's
             // last block is still copied to the host
             if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_out_free_[b].e, 0));
-            enqueue(stream_, frame_out_[b].as<float2>(), false, outs[k], false);
+            enqueue(stream_, frame_out_[b].as<float2>(), false, outs[k], false, true);
             BCSIM_CUDA(cudaEventRecord(ev_consumed_[b].e, stream_));
             BCSIM_CUDA(cudaEventRecord(ev_out_free_[b].e, copy_stream_.s));
         }

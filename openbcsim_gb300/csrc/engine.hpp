@@ -138,6 +138,14 @@ struct Plan {
     uint64_t records_key = 0;
 };
 
+// The shared-origin records of one simulation: sort keys and values, the
+// unsorted and the sorted record planes, the sort's scratch and the bin-range
+// counts, and the key of the records they hold.
+struct RecordSet {
+    DeviceBuffer keys_in, vals_in, keys_out, vals_out, recA, recB, records, sort_tmp, counts;
+    uint64_t key = 0;
+};
+
 // An event without timing, destroyed with its owner.
 struct OwnedEvent {
     cudaEvent_t e = nullptr;
@@ -181,7 +189,10 @@ public:
     // convolution runs in blocks of lines and each block's IQ is copied to
     // host_out on a copy stream while the next block is convolved; st then
     // waits for the copies unless wait_copies is false (ev_copied_ marks them).
-    void enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out = nullptr, bool wait_copies = true);
+    // staged: the bins (bins_[cur_]) are already cleared and the records
+    // (rs_[cur_]) prepared, with st waiting for both (simulate_fixed_frames).
+    void enqueue(cudaStream_t st, float2* dev_out, bool timing, float* host_out = nullptr, bool wait_copies = true,
+                 bool staged = false);
     // Copy the whole configuration of o (parameters, excitation, beam, scatterer
     // datasets -- device copies; not the scan sequence) into this simulator.
     void clone_from(Simulator& o);
@@ -206,8 +217,9 @@ public:
     // float4 xyza, replacing the fixed datasets) simulated into host IQ outs[k]
     // (cap_complex values each), as clear + add_fixed_scatterers +
     // simulate_lines per frame would, bit for bit.  Frame k+1's upload and
-    // amplitude bound run on their own stream while frame k is simulated.
-    // Afterwards the last frame is the fixed dataset.
+    // amplitude bound run on their own stream, and its bins clear and record
+    // preparation on another, while frame k is simulated (bins and records
+    // double-buffered).  Afterwards the last frame is the fixed dataset.
     void simulate_fixed_frames(const float* const* frames, int64_t n, int num_frames, float* const* outs,
                                int64_t cap_complex);
 
@@ -227,6 +239,10 @@ private:
     uint64_t records_key_of(const Plan& P) const;
     std::vector<double> data_shape() const;
     const float4* fixed_src() const { return fixed_src_ ? fixed_src_ : fixed_xyza_.as<float4>(); }
+    RecordSet& rec() { return rs_[cur_]; }
+    void reserve_records(RecordSet& R, Plan& P);
+    // record preparation (prep, sort, counts, gather) into rec(), on st
+    void enqueue_records(cudaStream_t st, int* launches);
 
     // configuration
     int device_ = 0;
@@ -236,7 +252,9 @@ private:
     OwnedStream copy_stream_;   // IQ copied to the host here while later lines are convolved
     OwnedStream upload_stream_;   // simulate_fixed_frames: the next frame's upload
     OwnedEvent ev_fork_, ev_join_, ev_copied_;
+    OwnedStream prep_stream_;     // simulate_fixed_frames: the next frame's bins clear and records
     OwnedEvent ev_uploaded_[2], ev_consumed_[2];   // per frame buffer: upload done / last reader done
+    OwnedEvent ev_staged_[2];   // a frame's bins cleared and records prepared
     std::vector<cudaEvent_t> ev_blocks_;   // one per convolution block (owned, see ~Simulator)
     PinnedInt flag_host_;
     cudaStream_t stream_ = nullptr;   // owned_stream_.s
@@ -266,7 +284,6 @@ private:
     uint64_t cfg_version_ = 1;   // bumped by every configuration change
     uint64_t static_version_ = 1;   // bumped by every change but new scatterer values
     uint64_t data_version_ = 1;  // bumped by every scatterer change
-    uint64_t records_key_ = 0;
     Plan plan_;
 
     bool excitation_set_ = false;
@@ -327,8 +344,11 @@ private:
     bool lines_valid_ = false;
     DeviceBuffer lines_dev_, line_order_dev_, cones_dev_;
     std::vector<int> line_rank_;   // position of each line in the direction-ordered sequence
-    DeviceBuffer bins_, out_;
-    DeviceBuffer keys_in_, vals_in_, keys_out_, vals_out_, recA_, recB_, records_, sort_tmp_, counts_;
+    // bins and records: set cur_ (the second set only for simulate_fixed_frames,
+    // whose next frame is cleared and prepared while the current one runs)
+    DeviceBuffer bins_[2], out_;
+    RecordSet rs_[2];
+    int cur_ = 0;
     DeviceBuffer gen_tiles_, gen_line_ids_, gen_basis_, spl_basis_d_, spl_basis_f_;
     std::vector<float> pinned_dummy_;
 
