@@ -387,7 +387,50 @@ def run_gpu(args):
     }
     if not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(job, args.cpu_seconds)
+    if world == 1 and not args.no_extras:
+        # the metric's other figures, each outside every timed region above:
+        # the timed output's IQ error against the FP64 oracle, the batched
+        # uneven jobs against plain execution, and the served request stream
+        # against serial plain execution
+        result["rel_rms"] = headline_rel_rms(job, dev_out.cpu().numpy())
+        del dev_out, flush, sim
+        torch.cuda.empty_cache()
+        result["batch"] = batch_section(args)
+        result["serve"] = serve_section(args)
     return result
+
+
+def headline_rel_rms(job, iq):
+    """Relative RMS of the timed step's IQ (the last timed simulation's output)
+    against the FP64 oracle over a spread of lines: 64 spread over the scan
+    plus, for a square grid of lines, its corners, edge middles and centre."""
+    from oracle import oracle as O
+
+    L = job.scan.num_lines
+    idx = [np.linspace(0, L - 1, 64).round().astype(int)]
+    n = int(round(np.sqrt(L)))
+    if n * n == L:
+        idx.append(np.array([0, n - 1, L - n, L - 1, n // 2, L - n + n // 2, (n // 2) * n, (n // 2) * n + n - 1,
+                             (n // 2) * n + n // 2]))
+    idx = np.unique(np.concatenate(idx))
+    t0 = time.perf_counter()
+    ref = O.simulate(_subset_idx(job, idx), O.MODE_FP64)
+    err = O.rel_rms(iq[idx], ref)
+    return {"value": err, "tolerance": 1e-4, "lines": int(len(idx)), "of_lines": L,
+            "reference": "FP64 CPU oracle (oracle/cole_oracle.c), same inputs",
+            "oracle_s": time.perf_counter() - t0}
+
+
+def _subset_idx(job, idx):
+    import copy
+
+    from openbcsim_gb300 import workloads as W
+
+    sub = copy.copy(job)
+    s = job.scan
+    sub.scan = W.ScanSequence(s.origins[idx], s.directions[idx], s.lateral_dirs[idx], s.timestamps[idx],
+                              s.line_length)
+    return sub
 
 
 STAGE_KEYS = ["kernel_memset_ms", "prep_sort_ms", "fixed_projection_kernel_ms", "spline_projection_kernel_ms",
@@ -480,11 +523,11 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "projections/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
-def run_batch(args):
+def batch_section(args):
     """Config 4: 64 uneven jobs (fixed and spline, uneven N, L, depth, pulse,
-    decimation).  plain: one simulate_lines per job, in order; batched: one
-    Batch.run (all jobs submitted at once on separate streams, replayed as a
-    CUDA graph).  Both with results on the host."""
+    decimation), results on the host.  plain: one simulate_lines per job, in
+    order (the one-simulation path); batched: one Batch.run.  Each form timed
+    over `batch_steps` runs after warm-up, host wall clock."""
     import torch
 
     import openbcsim_gb300 as gb
@@ -506,62 +549,66 @@ def run_batch(args):
             s.simulate_lines_line_major(o)
 
     batch = gb.Batch(sims, use_graph=True)
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         plain()
         batch.run(outs)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        plain()
-    t_plain = (time.perf_counter() - t0) / args.steps
+    steps = args.batch_steps
     clocks = ClockSampler(0)
     clocks.start()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
+        plain()
+    t_plain = (time.perf_counter() - t0) / steps
+    t0 = time.perf_counter()
+    for _ in range(steps):
         batch.run(outs)
-    t_batch = (time.perf_counter() - t0) / args.steps
+    t_batch = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
     n_spline = sum(1 for j in jobs if j.splines)
-    return {"metric": METRIC + " (batched uneven jobs)", "value": total / t_batch, "unit": "projections/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch * 1e3,
+    return {"workload": f"batch_uneven: {len(jobs)} jobs ({n_spline} spline), {total:.4e} projections per step, "
+                        f"scale {args.batch_scale}",
+            "unit": "projections/s", "steps": steps,
+            "batched": {"value": total / t_batch, "ms_per_step": t_batch * 1e3},
+            "plain": {"value": total / t_plain, "ms_per_step": t_plain * 1e3,
+                      "form": "one simulate_lines per job, in order, IQ to the host"},
+            "batched_over_plain": t_plain / t_batch, "io": "IQ to the host every step (both forms)",
+            "clocks": clk}
+
+
+def run_batch(args):
+    res = batch_section(args)
+    return {"metric": METRIC + " (batched uneven jobs)", "value": res["batched"]["value"], "unit": "projections/s",
+            "n_gpus": 1, "steps": res["steps"], "warmup": args.warmup, "ms_per_step": res["batched"]["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)",
-            "data": "synthetic (seeded)",
-            "config": {"workload": f"batch_uneven: {len(jobs)} jobs ({n_spline} spline), "
-                                   f"{total:.3e} projections per step, scale {args.batch_scale}",
-                       "l2": "jobs' data far exceed L2"},
-            "plain": {"value": total / t_plain, "ms_per_step": t_plain * 1e3},
-            "batched_over_plain": t_plain / t_batch, "clocks": clk}
+            "data": "synthetic (seeded)", "config": {"workload": res["workload"], "l2": "jobs' data far exceed L2"},
+            "plain": res["plain"], "batched_over_plain": res["batched_over_plain"], "clocks": res["clocks"]}
 
 
-def run_serve(args):
-    """Config 5: Poisson request stream over 8 resident phantoms, replayed in
-    real time against the continuous-batching server; the same stream run
-    serially (one plain simulate_lines at a time, each starting when the
-    previous one ended or when the request arrived) gives the serial latencies."""
-    import torch
+def _pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(round(q * (len(v) - 1))))] if v else None
+
+
+def serve_stream(args, phantoms, sims, rate, seconds):
+    """One Poisson stream (config 5) served live by the continuous-batching
+    server, then replayed live by serial plain execution (one simulate_lines
+    at a time in arrival order, each starting when the request has arrived and
+    the previous one is done).  Latency = arrival to result on the host."""
+    import queue
 
     import openbcsim_gb300 as gb
     from openbcsim_gb300 import workloads as W
 
-    torch.cuda.set_device(0)
-    phantoms = W.served_phantoms(scale=args.batch_scale)
-    reqs = W.request_stream(phantoms, rate_hz=args.rate, seconds=args.serve_seconds)
-    sims = []
-    for j in phantoms:
-        s = gb.RfSimulator("gpu")
-        gb.configure_job(s, j)
-        sims.append(s)
+    reqs = W.request_stream(phantoms, rate_hz=rate, seconds=seconds)
     server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4, max_in_flight=args.max_in_flight)
     pids = [server.add_phantom(s) for s in sims]
-    # warm-up: one request per phantom
-    for k, s in enumerate(phantoms):
+    for k, s in enumerate(phantoms):   # warm-up: one request per phantom
         sc = s.scan
         server.wait(server.submit(pids[k], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
                                   sc.timestamps, 8))
-    # a client: this thread submits at the stream's arrival times, a second one
+    # the client: this thread submits at the arrival times, a second one
     # collects the results in order as they complete
-    import queue
-
     ids = queue.Queue()
     lat = []
 
@@ -584,52 +631,66 @@ def run_serve(args):
     st = server.stats()
     server.close()
     n_proj = sum(phantoms[r.phantom].num_scatterers * r.scan.num_lines for r in reqs)
-    # serial plain execution of the same stream
-    service = []
+    # serial plain execution of the same stream, live
+    serial_lat, busy = [], 0.0
+    t_start = time.perf_counter()
     for r in reqs:
+        now = time.perf_counter() - t_start
+        if r.arrival > now:
+            time.sleep(r.arrival - now)
         s = sims[r.phantom]
         sc = r.scan
         t0 = time.perf_counter()
         s.set_parameter("radial_decimation", str(r.decimation))
         s.set_scan_sequence(sc.origins, sc.directions, sc.line_length, sc.lateral_dirs, sc.timestamps)
         s.simulate_lines_line_major()
-        service.append(time.perf_counter() - t0)
-    finish, serial_lat = 0.0, []
-    for r, sv in zip(reqs, service):
-        start = max(r.arrival, finish)
-        finish = start + sv
-        serial_lat.append((finish - r.arrival) * 1e3)
-    lat_sorted, ser_sorted = sorted(lat), sorted(serial_lat)
+        t1 = time.perf_counter()
+        busy += t1 - t0
+        serial_lat.append((t1 - t_start - r.arrival) * 1e3)
+    serial_wall = time.perf_counter() - t_start
+    return {"rate_hz": rate, "seconds": seconds, "requests": len(reqs),
+            "server": {"value": n_proj / wall, "wall_s": wall,
+                       "latency_ms": {"p50": _pct(lat, 0.5), "p99": _pct(lat, 0.99), "max": max(lat)},
+                       "completed": st["completed"], "failed": st["failed"]},
+            "serial_plain": {"value": n_proj / serial_wall, "wall_s": serial_wall, "busy_s": busy,
+                             "latency_ms": {"p50": _pct(serial_lat, 0.5), "p99": _pct(serial_lat, 0.99),
+                                            "max": max(serial_lat)}},
+            "server_over_serial_throughput": serial_wall / wall}
 
-    def pct(v, q):
-        return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
 
-    # where the tails come from: latency percentiles per phantom, and the slowest requests
-    per_phantom = {}
-    for k, ph in enumerate(phantoms):
-        idx = [i for i, r in enumerate(reqs) if r.phantom == k]
-        if not idx:
-            continue
-        a, b = sorted(lat[i] for i in idx), sorted(serial_lat[i] for i in idx)
-        per_phantom[ph.name] = {"requests": len(idx), "server_p50": pct(a, 0.5), "server_p99": pct(a, 0.99),
-                                "serial_p50": pct(b, 0.5), "serial_p99": pct(b, 0.99),
-                                "service_ms_mean": 1e3 * sum(service[i] for i in idx) / len(idx)}
-    slowest = sorted(range(len(reqs)), key=lambda i: -lat[i])[:8]
-    slow = [{"phantom": phantoms[reqs[i].phantom].name, "lines": reqs[i].scan.num_lines, "D": reqs[i].decimation,
-             "arrival_s": round(reqs[i].arrival, 4), "server_ms": lat[i], "serial_ms": serial_lat[i],
-             "service_ms": service[i] * 1e3} for i in slowest]
+def serve_section(args):
+    """Config 5 at the configured rate (200 requests/s) and at rates that load
+    the GPU, each stream `serve_seconds` long."""
+    import torch
 
-    return {"metric": METRIC + " (served stream)", "value": n_proj / wall, "unit": "projections/s",
-            "n_gpus": 1, "steps": len(reqs), "warmup": len(phantoms), "ms_per_step": wall * 1e3 / max(1, len(reqs)),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (time of flight f64)",
-            "data": "synthetic (seeded)",
-            "config": {"workload": f"served_stream: {len(reqs)} requests, Poisson {args.rate}/s over "
-                                   f"{args.serve_seconds} s, 8 resident phantoms (scale {args.batch_scale})",
-                       "max_in_flight": args.max_in_flight},
-            "latency_ms": {"p50": pct(lat_sorted, 0.5), "p99": pct(lat_sorted, 0.99), "max": lat_sorted[-1]},
-            "serial_plain": {"latency_ms": {"p50": pct(ser_sorted, 0.5), "p99": pct(ser_sorted, 0.99)},
-                             "busy_s": sum(service), "value": n_proj / sum(service)},
-            "server_stats": st, "per_phantom": per_phantom, "slowest_requests": slow}
+    import openbcsim_gb300 as gb
+    from openbcsim_gb300 import workloads as W
+
+    torch.cuda.set_device(0)
+    phantoms = W.served_phantoms(scale=args.batch_scale)
+    sims = []
+    for j in phantoms:
+        s = gb.RfSimulator("gpu")
+        gb.configure_job(s, j)
+        sims.append(s)
+    clocks = ClockSampler(0)
+    clocks.start()
+    streams = [serve_stream(args, phantoms, sims, float(r), args.serve_seconds) for r in args.rates.split(",")]
+    clk = clocks.stop()
+    return {"workload": "served_stream: Poisson arrivals over 8 resident phantoms (fixed 100k-2M, spline 50k-500k "
+                        "scatterers), 1-256 lines per request at random angles and times, decimation 4-16",
+            "unit": "projections/s", "max_in_flight": args.max_in_flight, "streams": streams, "clocks": clk}
+
+
+def run_serve(args):
+    res = serve_section(args)
+    top = res["streams"][-1]
+    return {"metric": METRIC + " (served stream)", "value": top["server"]["value"], "unit": "projections/s",
+            "n_gpus": 1, "steps": top["requests"], "warmup": 8, "ms_per_step": top["server"]["wall_s"] * 1e3 /
+            max(1, top["requests"]), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (time of flight f64)", "data": "synthetic (seeded)",
+            "config": {"workload": res["workload"], "max_in_flight": res["max_in_flight"]},
+            "streams": res["streams"], "clocks": res["clocks"]}
 
 
 def run_imaging(args):
@@ -709,8 +770,11 @@ def main():
                          "imaging: B-mode and colour-Doppler post-processing")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of N and L in batch/serve modes")
-    ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--rates", default="200,1000,3000", help="serve: request rates (req/s) of the streams")
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="single mode: leave out the rel_rms, batch and serve figures")
     ap.add_argument("--max-in-flight", type=int, default=3, help="serve mode: requests on the GPU at once")
     ap.add_argument("--simulate-only", action="store_true", help="only run warmup+steps simulations (profiling)")
     ap.add_argument("--traffic-bytes", type=float, default=None,

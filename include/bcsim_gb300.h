@@ -4,8 +4,8 @@
  * This is the drop-in boundary for the reference's algorithm interface
  * bcsim::IAlgorithm (src/core/LibBCSim.hpp:42-91) and its factory
  * bcsim::Create (src/core/LibBCSim.cpp:39-49), flattened to plain pointers and
- * sizes so that any FFI (ctypes, cgo, JNI, N-API) or the C++ adapter in
- * INTEGRATION.md can bind it.  Each function cites the reference member it
+ * sizes so that any FFI (ctypes, cgo, JNI, N-API) or the C++ IAlgorithm adapter
+ * (openbcsim_gb300/adapter/GB300Algorithm.hpp) can bind it.  Each function cites the reference member it
  * replaces.
  *
  * Conventions
@@ -56,7 +56,9 @@ const char* bcsim_last_error(const bcsim_handle* h);
  *   verbose, sound_speed, noise_amplitude, use_arc_projection, radial_decimation,
  *   phase_delay, gpu_device, cuda_streams, threads_per_block, store_kernel_details,
  * plus this engine's own keys:
- *   precision_mode ("fp64" | "reference"), fir_tail_energy, tile_lines, autotune. */
+ *   precision_mode ("fp64" | "reference"), fir_tail_energy, convolution ("auto" | "fir" | "fft"),
+ *   tile_lines, autotune, cull, record_cache, render_once (splines at one shared
+ *   timestamp and origin rendered once, the reference's GpuAlgorithm.cpp:181-187). */
 int bcsim_set_parameter(bcsim_handle* h, const char* key, const char* value);
 
 /* IAlgorithm::get_parameter (GpuAlgorithm.cpp:761-773): num_cuda_devices,
@@ -155,6 +157,16 @@ int bcsim_get_debug_data(const bcsim_handle* h, const char* key, double* out, in
 typedef void (*bcsim_log_fn)(int level, const char* message, void* user);
 int bcsim_set_logger(bcsim_handle* h, bcsim_log_fn fn, void* user);
 
+/* Fault injection for tests (no counterpart in the reference).  The engine's
+ * kernels wait for their asynchronous copies with bounded waits; one that gives
+ * up sets the handle's device error flag and returns, and the next call that
+ * synchronises with the result (bcsim_simulate_lines, the frames, packet and
+ * imaging calls, a batch run) fails with BCSIM_E_INTERNAL ("a bounded device
+ * wait gave up; results are incomplete") and clears the flag.  This sets the
+ * flag from the host, as such a wait would, so that the error path can be
+ * tested without any device fault. */
+int bcsim_debug_raise_wait_flag(bcsim_handle* h);
+
 /* ---------------------------------------------------------------------------
  * Batched simulation (the reference has none: its GPU algorithm runs one
  * simulation per simulate_lines call, one line at a time, GpuAlgorithm.cpp:189-265).
@@ -207,10 +219,28 @@ int bcsim_server_submit(bcsim_server* s, int phantom_id, const float* origins, c
  * and releases the request; latency_ms = submit to result on the host. */
 int bcsim_server_wait(bcsim_server* s, int64_t request_id, float* out, int64_t cap_complex, int64_t* num_lines,
                       int64_t* num_samples, double* latency_ms, int timeout_ms);
+/* Admission by device memory: a request is admitted when a slot of its
+ * phantom is free (or can be made within the budget) and the device memory its
+ * slot has to grow by is available (free device memory plus the stream-ordered
+ * pool's reserved-but-unused bytes, less 256 MiB).  A request that does not fit
+ * waits while others are in flight; one that cannot fit with nothing in flight,
+ * or whose footprint exceeds hbm_budget_bytes, fails with BCSIM_E_MEMORY.  A
+ * request whose scan or timestamps are invalid fails with the reference's
+ * message; the others are unaffected. */
 /* Counters: completed and failed requests, latency percentiles over completed
  * requests, projections done, device bytes held by slots, queued requests. */
 int bcsim_server_stats(bcsim_server* s, int64_t* completed, int64_t* failed, double* p50_ms, double* p99_ms,
                        int64_t* projections, int64_t* hbm_in_use, int64_t* queue_depth);
+/* Fault injection for tests, all on the host: WAIT_FLAG raises the device
+ * error flag of the next admitted request's slot (as a bounded wait that gave
+ * up would: that request fails with BCSIM_E_INTERNAL); WORKER_THROW makes the
+ * worker's next dispatch throw (that request fails with BCSIM_E_INTERNAL,
+ * "injected worker failure"); FREE_MEMORY_CAP caps the device memory that
+ * admission sees at `value` bytes (value < 0 removes the cap). */
+#define BCSIM_SERVER_INJECT_WAIT_FLAG 1
+#define BCSIM_SERVER_INJECT_WORKER_THROW 2
+#define BCSIM_SERVER_INJECT_FREE_MEMORY_CAP 3
+int bcsim_server_debug_inject(bcsim_server* s, int what, int64_t value);
 
 /* Allocation-free simulation (no counterpart in the reference).
  *
@@ -222,14 +252,17 @@ int bcsim_server_stats(bcsim_server* s, int64_t* completed, int64_t* failed, dou
  * output d_out (device, complex64 [num_lines][ceil(ns / radial_decimation)]);
  * the scan lines and excitation are host arrays as in bcsim_set_scan_sequence /
  * bcsim_set_excitation.  All intermediates live in one static device array of
- * 32 MiB that every GPU loading this library holds until exit.  Limits:
+ * about 31.3 MiB that every GPU loading this library holds until exit.  Limits:
  * num_lines <= 4096, num_lines * ns * (phase_delay ? 2 : 1) <= 3932160,
  * ns + num_samples - 1 <= 65536.  amplitude_sum_bound must bound sum |a|
- * (it sets the fixed-point scale of the bins).  The first call on each device
- * looks up the static array's address (make it before any stream capture).
- * Calls share the array: calls that overlap on the GPU race, so issue them on
- * one stream.  Returns when the IQ is in d_out; on failure a message is written
- * to err (err_cap bytes). */
+ * (it sets the fixed-point scale of the bins): a bound below the measured sum
+ * fails the call, and so does a non-finite amplitude ("Nan in scatterer
+ * projection."), both before anything is written.  d_xyza and d_out must be
+ * device (or managed) memory of the current device.  The first call on each
+ * device looks up the static array's address (make it before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race, so
+ * issue them on one stream.  The call is synchronous: it returns once the IQ
+ * is in d_out.  On failure a message is written to err (err_cap bytes). */
 int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const float* origins, const float* directions,
                                  const float* lateral_dirs, int num_lines, float line_length, float sound_speed,
                                  const float* samples, int num_samples, int center_index, float sampling_frequency,

@@ -295,6 +295,11 @@ class RfSimulator:
                                                                ip))
         return r0, vel, img
 
+    def debug_raise_wait_flag(self):
+        """Test hook: set the device error flag as a bounded wait that gave up
+        would; the next synchronising call fails and clears it."""
+        self._check(self._lib.bcsim_debug_raise_wait_flag(self._h))
+
     def set_logger(self, fn):
         """fn(level: int, message: str) receives the engine's log messages; None silences."""
         if fn is None:
@@ -333,6 +338,10 @@ def configure_job(sim: RfSimulator, job, precision_mode: str = "fp64"):
     sim.set_parameter("phase_delay", "on" if job.phase_delay else "off")
     sim.set_parameter("radial_decimation", str(job.decimation))
     sim.set_parameter("precision_mode", precision_mode)
+    if getattr(job, "noise_amplitude", 0.0):
+        sim.set_parameter("noise_amplitude", repr(float(job.noise_amplitude)))
+        # the seed resets the simulator's frame counter; its next simulation draws frame 0
+        sim.set_parameter("noise_seed", str(int(job.noise_seed)))
     sim.set_excitation(job.taps, job.center_index, job.fs, job.demod_freq)
     s = job.scan
     sim.set_scan_sequence(s.origins, s.directions, s.line_length, s.lateral_dirs, s.timestamps)
@@ -444,6 +453,12 @@ class Server:
         self._check(rc)
         self._shapes.pop(request_id, None)
         return buf[: nl.value * nd.value].reshape(nl.value, nd.value).copy(), lat.value
+
+    INJECT_WAIT_FLAG, INJECT_WORKER_THROW, INJECT_FREE_MEMORY_CAP = 1, 2, 3
+
+    def debug_inject(self, what: int, value: int = 0):
+        """Test hook (bcsim_server_debug_inject): host-side fault injection."""
+        self._check(self._lib.bcsim_server_debug_inject(self._s, int(what), int(value)))
 
     def stats(self) -> dict:
         c, f, q, pr, hb, qd = (C.c_int64() for _ in range(6))

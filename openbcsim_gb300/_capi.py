@@ -44,6 +44,7 @@ SIGNATURES = [
     ("bcsim_get_stream", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bcsim_get_debug_data", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64, _i64p]),
     ("bcsim_set_logger", C.c_int, [C.c_void_p, LOG_FN, C.c_void_p]),
+    ("bcsim_debug_raise_wait_flag", C.c_int, [C.c_void_p]),
     ("bcsim_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     ("bcsim_batch_destroy", C.c_int, [C.c_void_p]),
     ("bcsim_batch_last_error", C.c_char_p, [C.c_void_p]),
@@ -60,6 +61,7 @@ SIGNATURES = [
                                     C.POINTER(C.c_double), C.c_int]),
     ("bcsim_server_stats", C.c_int, [C.c_void_p, _i64p, _i64p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                      _i64p, _i64p, _i64p]),
+    ("bcsim_server_debug_inject", C.c_int, [C.c_void_p, C.c_int, C.c_int64]),
     ("bcsim_bmode_image", C.c_int, [C.c_void_p, _f32p, C.c_int64, C.c_int64, C.c_float, C.c_float, C.c_float,
                                     C.c_void_p, C.c_void_p, C.c_void_p, _f32p]),
     ("bcsim_simulate_bmode", C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_void_p,

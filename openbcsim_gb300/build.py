@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 
 CU_SOURCES = ["project.cu", "conv.cu", "fftconv.cu", "noalloc.cu", "ingest.cu", "imaging.cu"]
 CPP_SOURCES = ["engine.cpp", "host_dsp.cpp", "capi.cpp", "batch.cpp", "server.cpp", "imaging_host.cpp"]
-HEADERS = ["kernels.hpp", "dfloat.cuh", "fixedpoint.cuh", "async_copy.cuh", "engine.hpp", "host_dsp.hpp", "imaging.hpp", "imaging_host.hpp"]
+HEADERS = ["kernels.hpp", "dfloat.cuh", "fixedpoint.cuh", "async_copy.cuh", "noise.cuh", "engine.hpp", "host_dsp.hpp", "imaging.hpp", "imaging_host.hpp"]
 
 HOST_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-std=c++17", "-Wall", "-Wno-unused-function", "-pthread"]
 

@@ -83,8 +83,11 @@ void run(bcsim_batch* b, const std::vector<float2*>& outs) {
         }
     }
     // the first run after a change is submitted directly: it also produces the
-    // records the later (captured) runs reuse
-    if (!b->use_graph || b->runs_since_change == 0) {
+    // records the later (captured) runs reuse.  Simulators with seeded noise
+    // draw a new frame every run, which a graph replay would not: no graph then
+    bool noisy = false;
+    for (size_t i = 0; i < n; i++) noisy = noisy || bcsim_gb300::simulator_of(b->handles[i]).noisy();
+    if (!b->use_graph || b->runs_since_change == 0 || noisy) {
         enqueue_all(b, outs);
         b->runs_since_change++;
         return;

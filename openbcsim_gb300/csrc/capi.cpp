@@ -305,6 +305,10 @@ int bcsim_simulate_color_doppler(bcsim_handle* h, int packet_size, float prt, fl
     });
 }
 
+int bcsim_debug_raise_wait_flag(bcsim_handle* h) {
+    return guarded(h, [&] { h->sim.raise_device_flag(); });
+}
+
 int bcsim_set_logger(bcsim_handle* h, bcsim_log_fn fn, void* user) {
     return guarded(h, [&] { h->sim.set_logger(fn, user); });
 }

@@ -48,6 +48,7 @@
 #include <cuda_runtime.h>
 #include "kernels.hpp"
 #include "fixedpoint.cuh"
+#include "noise.cuh"
 
 namespace bcsim_gb300 {
 
@@ -166,13 +167,16 @@ __device__ __forceinline__ void fir_store(const float2 ys[4], int64_t line, int 
 
 // One work item per CTA: line blockIdx.y, outputs blockIdx.x * blockDim.x * 4 ...
 // (at most 102 registers: 96 in the complex-bin kernel, so that an SM holds 20
-// warps -- six 96-thread CTAs, their shared memory permitting -- not 16)
-template <bool PD, bool TAPS_SMEM>
+// warps -- six 96-thread CTAs, their shared memory permitting -- not 16).
+// PD: the bins are complex (phase delay); NZ: seeded noise is added to every
+// staged bin j < ns (noise.cuh), which makes real bins complex too.
+template <bool PD, bool TAPS_SMEM, bool NZ>
 __global__ void __launch_bounds__(128, 5)
     convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale,
                                const float2* __restrict__ taps_pm, const int* __restrict__ ph_off, int W,
                                int tap_start, int64_t M, int center, int D, int nd, int sub, int row, int cols,
-                               const float2* __restrict__ demod, float2* __restrict__ out) {
+                               const float2* __restrict__ demod, float2* __restrict__ out, NoiseParams nz) {
+    constexpr bool CX = PD || NZ;   // complex arithmetic
     extern __shared__ __align__(16) float4 smem4[];
     float2* seg = reinterpret_cast<float2*>(smem4);   // [D][row]
     // phase-major taps, in shared memory when they fit
@@ -184,7 +188,7 @@ __global__ void __launch_bounds__(128, 5)
     if (TAPS_SMEM) {
         const int ntaps_pm = __ldg(ph_off + D);
         for (int i = tid; i < ntaps_pm; i += blockDim.x)
-            tp4[i] = PD ? tap_split(__ldg(taps_pm + i)) : tap_real(__ldg(taps_pm + i));
+            tp4[i] = CX ? tap_split(__ldg(taps_pm + i)) : tap_real(__ldg(taps_pm + i));
     }
     const long long jbase = (long long)center + (long long)m0 * D - tap_start - (W - 1);
     const long long mmask = (long long)M - 1;
@@ -202,11 +206,13 @@ __global__ void __launch_bounds__(128, 5)
     int col_t = tid / D, ph_t = tid - col_t * D;   // (column, phase) of element q0
     for (int q0 = tid; q0 < nelem; q0 += 8 * blockDim.x) {
         longlong2 v[8];
+        int jj[NZ ? 8 : 1];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const int q = q0 + u * (int)blockDim.x;
             const long long j = (jbase + q) & mmask;
             v[u] = make_longlong2(0, 0);
+            if (NZ) jj[u] = (q < nelem && j < ns) ? (int)j : -1;
             if (q < nelem && j < ns) {
                 if (PD) v[u] = __ldg(reinterpret_cast<const longlong2*>(lb) + j);
                 else v[u].x = __ldg(lb + j);
@@ -215,9 +221,15 @@ __global__ void __launch_bounds__(128, 5)
         int c = col_t, p = ph_t;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-            if (q0 + u * (int)blockDim.x < nelem)
-                seg[p * row + (c & 3) * sub + (c >> 2)] =
-                    make_float2(fix2f(v[u].x, inv_scale), PD ? fix2f(v[u].y, inv_scale) : 0.0f);
+            if (q0 + u * (int)blockDim.x < nelem) {
+                float2 val = make_float2(fix2f(v[u].x, inv_scale), PD ? fix2f(v[u].y, inv_scale) : 0.0f);
+                if (NZ && jj[u] >= 0) {
+                    const float2 n = bin_noise(nz, nz.line0 + line, jj[u]);
+                    val.x += n.x;
+                    val.y += n.y;
+                }
+                seg[p * row + (c & 3) * sub + (c >> 2)] = val;
+            }
             c += step_c;
             p += step_p;
             if (p >= D) { p -= D; c++; }
@@ -229,7 +241,7 @@ __global__ void __launch_bounds__(128, 5)
     __syncthreads();
     if (tid * CONV_K >= valid) return;   // no output of this thread (no barrier follows)
     float2 ys[CONV_K];
-    fir_mac<PD, TAPS_SMEM>(seg, row, sub, tid, tp4, taps_pm, ph_off, D, ys);
+    fir_mac<CX, TAPS_SMEM>(seg, row, sub, tid, tp4, taps_pm, ph_off, D, ys);
     fir_store(ys, line, m0, tid, nd, demod, out);
 }
 
@@ -249,9 +261,13 @@ static int conv_row(int cols) {
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                        float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
                                        int max_ph_taps, int W, int tap_start, int64_t M, int center, int decimation,
-                                       int nd, const float2* demod, float2* out, cudaStream_t stream) {
+                                       int nd, const float2* demod, float2* out, cudaStream_t stream,
+                                       const NoiseParams* noise) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
     if (max_ph_taps % 4) return cudaErrorInvalidValue;
+    NoiseParams nz{};
+    const bool noisy = noise && noise->sigma > 0.0f;
+    if (noisy) nz = *noise;
     const int D = decimation;
     int dev = 0, sms = 0, smem_optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -290,12 +306,19 @@ cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_l
         cudaError_t e2 = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e2 != cudaSuccess) return e2;
         k<<<grid, threads, smem, stream>>>(bins, ns, inv_scale, taps_pm, ph_off, W, tap_start, M, center, D, nd, sub,
-                                           row, cols, demod, out);
+                                           row, cols, demod, out, nz);
         return cudaGetLastError();
     };
-    if (phase_delay) return taps_in_smem ? launch(convolve_demodulate_kernel<true, true>)
-                                         : launch(convolve_demodulate_kernel<true, false>);
-    return taps_in_smem ? launch(convolve_demodulate_kernel<false, true>) : launch(convolve_demodulate_kernel<false, false>);
+    if (noisy) {
+        if (phase_delay) return taps_in_smem ? launch(convolve_demodulate_kernel<true, true, true>)
+                                             : launch(convolve_demodulate_kernel<true, false, true>);
+        return taps_in_smem ? launch(convolve_demodulate_kernel<false, true, true>)
+                            : launch(convolve_demodulate_kernel<false, false, true>);
+    }
+    if (phase_delay) return taps_in_smem ? launch(convolve_demodulate_kernel<true, true, false>)
+                                         : launch(convolve_demodulate_kernel<true, false, false>);
+    return taps_in_smem ? launch(convolve_demodulate_kernel<false, true, false>)
+                        : launch(convolve_demodulate_kernel<false, false, false>);
 }
 
 int make_phase_major_taps(const float2* taps, int W, int D, float2* out, int* off, int* max_ph) {

@@ -117,6 +117,8 @@ void Simulator::ensure_device() {
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_join_.e, cudaEventDisableTiming));
     BCSIM_CUDA(cudaEventCreateWithFlags(&ev_copied_.e, cudaEventDisableTiming));
     stream_ = owned_stream_.s;
+    err_flag_dev_.reserve(sizeof(int));
+    BCSIM_CUDA(cudaMemset(err_flag_dev_.get(), 0, sizeof(int)));
     device_ready_ = true;
     {
         // the device pool behind the stream-ordered buffers keeps freed memory
@@ -161,9 +163,14 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
         if (v <= 0) throw SimError(BCSIM_E_INVALID, "illegal sound speed");
         sound_speed_ = v;
     } else if (key == "noise_amplitude") {
+        // BaseAlgorithm.cpp:58-60: any float; noise is added when it is > 0
         const float v = std::stof(value);
-        if (v != 0.0f) throw SimError(BCSIM_E_INVALID, "noise_amplitude: only 0 is supported by this engine");
+        if (!std::isfinite(v)) throw SimError(BCSIM_E_INVALID, "noise_amplitude must be finite");
         noise_amplitude_ = v;
+    } else if (key == "noise_seed") {
+        // the seed of the counter-based noise; setting it restarts the frame counter
+        noise_seed_ = std::stoull(value);
+        noise_frame_ = 0;
     } else if (key == "use_arc_projection") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         arc_ = b;
@@ -232,6 +239,9 @@ void Simulator::set_parameter(const std::string& key, const std::string& value) 
     } else if (key == "cull") {
         if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
         cull_ = b;
+    } else if (key == "render_once") {
+        if (!parse_bool(value, &b)) throw SimError(BCSIM_E_INVALID, "invalid boolean value");
+        render_once_ = b;
     } else if (key == "tile_lines") {
         const int v = std::stoi(value);
         if (v < 0) throw SimError(BCSIM_E_INVALID, "tile_lines must be >= 0");
@@ -255,6 +265,9 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "verbose") return std::to_string(verbose_);
     if (key == "sound_speed") return fmt_double(sound_speed_);
     if (key == "noise_amplitude") return fmt_double(noise_amplitude_);
+    if (key == "noise_seed") return std::to_string(noise_seed_);
+    // the frame number the next simulation draws its noise for
+    if (key == "noise_frame") return std::to_string(noise_frame_);
     if (key == "use_arc_projection") return arc_ ? "on" : "off";
     if (key == "radial_decimation") return std::to_string(decimation_);
     if (key == "phase_delay") return phase_delay_ ? "on" : "off";
@@ -269,6 +282,7 @@ std::string Simulator::get_parameter(const std::string& key) const {
     if (key == "convolution_route") return route_known_ ? (last_route_fft_ ? "fft" : "fir") : "";
     if (key == "tile_lines") return std::to_string(tile_lines_);
     if (key == "cull") return cull_ ? "on" : "off";
+    if (key == "render_once") return render_once_ ? "on" : "off";
     if (key == "record_cache") return record_cache_ ? "on" : "off";
     if (key == "wide_cta") return wide_cta_ ? "on" : "off";
     if (key == "lut_smem") return lut_smem_ ? "on" : "off";
@@ -960,6 +974,7 @@ void Simulator::prepare() {
     set_fixed_point_scale(p);
     p.wide_cta = wide_cta_ ? 1 : 0;
     p.lut_smem = lut_smem_ ? 1 : 0;
+    p.err_flag = err_flag_dev_.as<int>();
     // exact culling ranges (fp64 mode): outside them the weight is exactly 0
     if (mode_ == MODE_FP64 && cull_) {
         double llo, lhi, elo, ehi;
@@ -1020,7 +1035,7 @@ void Simulator::prepare() {
     // splines go through the shared path when every line sees them at one time
     P.spline_shared.assign(splines_.size(), 0);
     P.n_shared = P.shared ? fixed_n_ : 0;
-    if (P.shared && timestamps_equal_) {
+    if (P.shared && timestamps_equal_ && render_once_) {
         for (size_t d = 0; d < splines_.size(); d++) {
             if (splines_[d].n > 0) {
                 P.spline_shared[d] = 1;
@@ -1315,22 +1330,32 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         ev_blocks_.push_back(e);
     }
     const int stride_bins = p.phase_delay ? 2 : 1;
+    // seeded noise on the time projection (noise_amplitude > 0), keyed by the
+    // seed, this simulation's frame number, the line and the sample
+    NoiseParams nz{};
+    if (noise_amplitude_ > 0.0f) {
+        nz.sigma = noise_amplitude_;
+        nz.key0 = (uint32_t)noise_seed_;
+        nz.key1 = (uint32_t)(noise_seed_ >> 32);
+        nz.frame = noise_frame_++;
+    }
     for (int k = 0; k < nblocks; k++) {
         const int l0 = (int)((int64_t)L * k / nblocks), l1 = (int)((int64_t)L * (k + 1) / nblocks);
         if (l1 <= l0) continue;
+        nz.line0 = l0;
         ++launches;
         if (use_fft)
             BCSIM_CUDA(launch_fft_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns,
                                                       p.phase_delay, std::ldexp(1.0f, -p.log2scale),
                                                       fft_spec_dev_.as<float2>(), fft_tw_dev_.as<float2>(), M_,
                                                       decimation_, (int)nd_, demod_dev_.as<float2>(),
-                                                      dev_out + (int64_t)l0 * nd_, st));
+                                                      dev_out + (int64_t)l0 * nd_, st, &nz));
         else
             BCSIM_CUDA(launch_convolve_demodulate(bins + (int64_t)l0 * ns * stride_bins, l1 - l0, ns, p.phase_delay,
                                                   std::ldexp(1.0f, -p.log2scale), taps_pm_dev_.as<float2>(),
                                                   ph_off_dev_.as<int>(), ntaps_pm_, max_ph_taps_, (int)tap_count_,
                                                   (int)tap_start_, M_, center_, decimation_, (int)nd_,
-                                                  demod_dev_.as<float2>(), dev_out + (int64_t)l0 * nd_, st));
+                                                  demod_dev_.as<float2>(), dev_out + (int64_t)l0 * nd_, st, &nz));
         if (host_out) {
             const cudaStream_t cs = copy_stream_.s;
             BCSIM_CUDA(cudaEventRecord(ev_blocks_[k], st));
@@ -1369,7 +1394,7 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
         // (the IQ was copied by enqueue, overlapped with the convolution)
         // the bounded-wait error flag travels with the result (one synchronisation)
         if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
-        BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, st));
+        BCSIM_CUDA(enqueue_error_flag_read(err_flag_dev_.as<int>(), flag_host_.p, st));
         BCSIM_CUDA(cudaStreamSynchronize(st));
         if (store_details_) debug_["kernel_memcpy_ms"].push_back(timer.stop());
         if (*flag_host_.p) check_device_flag();   // clears the flag and reports
@@ -1377,9 +1402,17 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
 }
 
 void Simulator::check_device_flag() {
+    ensure_device();
     int flag = 0;
-    BCSIM_CUDA(read_and_clear_error_flag(&flag, stream_));
+    BCSIM_CUDA(read_and_clear_error_flag(err_flag_dev_.as<int>(), &flag, stream_));
     if (flag) throw SimError(BCSIM_E_INTERNAL, "a bounded device wait gave up; results are incomplete");
+}
+
+void Simulator::raise_device_flag() {
+    ensure_device();
+    const int one = 1;
+    BCSIM_CUDA(cudaMemcpyAsync(err_flag_dev_.get(), &one, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));
 }
 
 // Lines-per-tile and records-per-CTA from measurement: every candidate launch
@@ -1532,7 +1565,7 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
         }
         BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_copied_.e, 0));   // the last frame's copies
         if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
-        BCSIM_CUDA(enqueue_error_flag_read(flag_host_.p, stream_));
+        BCSIM_CUDA(enqueue_error_flag_read(err_flag_dev_.as<int>(), flag_host_.p, stream_));
     } catch (...) {
         settle();
         throw;
@@ -1599,6 +1632,8 @@ void Simulator::clone_from(Simulator& o) {
     verbose_ = o.verbose_;
     sound_speed_ = o.sound_speed_;
     noise_amplitude_ = o.noise_amplitude_;
+    noise_seed_ = o.noise_seed_;
+    noise_frame_ = 0;
     arc_ = o.arc_;
     decimation_ = o.decimation_;
     phase_delay_ = o.phase_delay_;
@@ -1609,6 +1644,7 @@ void Simulator::clone_from(Simulator& o) {
     convolution_ = o.convolution_;
     tile_lines_ = o.tile_lines_;
     cull_ = o.cull_;
+    render_once_ = o.render_once_;
     record_cache_ = o.record_cache_;
     autotune_ = o.autotune_;
     wide_cta_ = o.wide_cta_;

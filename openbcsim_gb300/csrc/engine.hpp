@@ -206,7 +206,19 @@ public:
     int64_t num_out_samples() const { return nd_; }
     float2* internal_output() { return out_.as<float2>(); }
     uint64_t config_version() const { return cfg_version_; }
+    // Seeded noise on: every simulation draws the next frame's noise (a
+    // captured graph would replay one frame's).
+    bool noisy() const { return noise_amplitude_ > 0.0f; }
+    // Throws if a bounded device wait of this simulator's kernels gave up since
+    // the last check (and clears the flag).
     void check_device_flag();
+    // Test hook: sets the device error flag as a bounded wait that gave up
+    // would (host-side injection; no kernel is involved).
+    void raise_device_flag();
+    // Copy of the device error flag into host_flag (pinned), in st's order.
+    cudaError_t enqueue_flag_read(int* host_flag, cudaStream_t st) {
+        return enqueue_error_flag_read(err_flag_dev_.as<int>(), host_flag, st);
+    }
     void simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples);
     void simulate_device(void* dev_out, int64_t cap_complex);
     // A colour-Doppler packet (MainWindow.cpp:664-694): P frames of the scan,
@@ -257,10 +269,13 @@ private:
     OwnedEvent ev_staged_[2];   // a frame's bins cleared and records prepared
     std::vector<cudaEvent_t> ev_blocks_;   // one per convolution block (owned, see ~Simulator)
     PinnedInt flag_host_;
+    DeviceBuffer err_flag_dev_;   // this simulator's device error flag (SimParams::err_flag)
     cudaStream_t stream_ = nullptr;   // owned_stream_.s
     int verbose_ = 0;
     float sound_speed_ = 1540.0f;
     float noise_amplitude_ = 0.0f;
+    uint64_t noise_seed_ = 0;
+    uint32_t noise_frame_ = 0;   // frame number of the next simulation's noise
     bool arc_ = true;
     int decimation_ = 1;
     bool phase_delay_ = false;
@@ -272,6 +287,10 @@ private:
     int convolution_ = 0;   // 0 = automatic, 1 = direct FIR, 2 = FFT
     int tile_lines_ = 0;   // 0 = automatic
     bool cull_ = true;     // exact culling of zero-weight (scatterer, line-slot) pairs
+    // splines seen by every line at one time from one origin are rendered once
+    // into shared-origin records (the reference's render at a common timestamp,
+    // GpuAlgorithm.cpp:181-187); off: the per-pair path evaluates them per line
+    bool render_once_ = true;
     bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
     bool autotune_ = false;
     bool wide_cta_ = true;       // shared-origin kernel launch shape (see launch_project_shared)

@@ -47,6 +47,7 @@
 #include <type_traits>
 #include <vector>
 #include "fixedpoint.cuh"
+#include "noise.cuh"
 #include "kernels.hpp"
 
 namespace bcsim_gb300 {
@@ -241,14 +242,24 @@ __device__ __forceinline__ void fft_middle(float2* s, int M, const float4* __res
     }
 }
 
+// Bin n of a line as float, plus its seeded noise (noise.cuh) when nz.sigma > 0.
 template <bool PD>
-__device__ __forceinline__ float2 load_bin(const long long* __restrict__ lb, int n, int ns, float inv_scale) {
+__device__ __forceinline__ float2 load_bin(const long long* __restrict__ lb, int n, int ns, float inv_scale,
+                                           const NoiseParams& nz, int line) {
     if (n >= ns) return make_float2(0.0f, 0.0f);
+    float2 v;
     if (PD) {
-        const longlong2 v = __ldg(reinterpret_cast<const longlong2*>(lb) + n);
-        return make_float2(fix2f(v.x, inv_scale), fix2f(v.y, inv_scale));
+        const longlong2 q = __ldg(reinterpret_cast<const longlong2*>(lb) + n);
+        v = make_float2(fix2f(q.x, inv_scale), fix2f(q.y, inv_scale));
+    } else {
+        v = make_float2(fix2f(__ldg(lb + n), inv_scale), 0.0f);
     }
-    return make_float2(fix2f(__ldg(lb + n), inv_scale), 0.0f);
+    if (nz.sigma > 0.0f) {   // uniform over the CTA
+        const float2 e = bin_noise(nz, nz.line0 + line, n);
+        v.x += e.x;
+        v.y += e.y;
+    }
+    return v;
 }
 
 // One line per CTA.  Passes: forward radix 16 at L = M (from the bins), radix
@@ -260,7 +271,8 @@ template <int RS, bool PD, int MINB>
 __global__ void __launch_bounds__(FFT_THREADS, MINB)
     fft_convolve_demodulate_kernel(const unsigned long long* __restrict__ bins, int ns, float inv_scale, int M,
                                    int F, const float4* __restrict__ spec4, const float2* __restrict__ tw, int D,
-                                   int nd, const float2* __restrict__ demod, float2* __restrict__ out) {
+                                   int nd, const float2* __restrict__ demod, float2* __restrict__ out,
+                                   NoiseParams nz) {
     extern __shared__ __align__(16) float2 s[];
     const int Mp = M / F;
     float2* tq = s + fpad(M);   // W_M^y, y < M/4 (complete at the barrier after pass 0)
@@ -277,7 +289,7 @@ __global__ void __launch_bounds__(FFT_THREADS, MINB)
             float2 v[16];
             const TaskTw w = task_twiddles_global(tw, t);
 #pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = load_bin<PD>(lb, t + j * S, ns, inv_scale);
+            for (int j = 0; j < 16; j++) v[j] = load_bin<PD>(lb, t + j * S, ns, inv_scale, nz, line);
             dft<16, false>(v);
 #pragma unroll
             for (int q = 0; q < 16; q++) {
@@ -390,8 +402,10 @@ void make_fft_tables(const std::complex<double>* H, int64_t M, int center, float
 cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                            float inv_scale, const float2* spec, const float2* tw, int64_t M,
                                            int decimation, int nd, const float2* demod, float2* out,
-                                           cudaStream_t stream) {
+                                           cudaStream_t stream, const NoiseParams* noise) {
     if (num_lines <= 0 || nd <= 0) return cudaSuccess;
+    NoiseParams nz{};
+    if (noise && noise->sigma > 0.0f) nz = *noise;
     if (!fft_convolution_supported(M) || ns > M) return cudaErrorInvalidValue;
     const int F = fft_fold(decimation);
     const size_t smem = fft_convolution_smem(M);
@@ -402,7 +416,7 @@ cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int n
         if (e != cudaSuccess) return e;
         k<<<num_lines, FFT_THREADS, smem, stream>>>(bins, ns, inv_scale, (int)M, F,
                                                    reinterpret_cast<const float4*>(spec), tw, decimation, nd, demod,
-                                                   out);
+                                                   out, nz);
         return cudaGetLastError();
     };
     auto pick = [&](auto pd) -> cudaError_t {

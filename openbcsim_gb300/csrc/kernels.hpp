@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "noise.cuh"
+
 namespace bcsim_gb300 {
 
 // One scan line as the kernels see it: origin, radial, lateral and elevational
@@ -57,6 +59,7 @@ struct SimParams {
     int wide_cta;              // shared-origin kernel: 1024/512-thread CTAs for >= 512 lines
     int lut_smem;              // wide shared-origin kernel: lookup-table planes in shared memory
     int fold;                  // shared-origin kernel: FP32 run sums folded at record indices k*fold (power of 2)
+    int* err_flag;             // the simulator's device error flag: set to 1 when a bounded wait gives up (may be null)
 };
 
 // Frame spread of a slot of 32 lines (consecutive in the kernel's line order):
@@ -171,7 +174,8 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
 cudaError_t launch_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                        float inv_scale, const float2* taps_pm, const int* ph_off, int ntaps_pm,
                                        int max_ph_taps, int num_taps, int tap_start, int64_t M, int center,
-                                       int decimation, int nd, const float2* demod, float2* out, cudaStream_t stream);
+                                       int decimation, int nd, const float2* demod, float2* out, cudaStream_t stream,
+                                       const NoiseParams* noise = nullptr);
 
 // The same by FFT (fftconv.cu): the full length-M circular convolution with
 // the analytic pulse, one line per CTA in shared memory, for power-of-two
@@ -190,7 +194,7 @@ void make_fft_tables(const std::complex<double>* H, int64_t M, int center, float
 cudaError_t launch_fft_convolve_demodulate(const unsigned long long* bins, int num_lines, int ns, int phase_delay,
                                            float inv_scale, const float2* spec, const float2* tw, int64_t M,
                                            int decimation, int nd, const float2* demod, float2* out,
-                                           cudaStream_t stream);
+                                           cudaStream_t stream, const NoiseParams* noise = nullptr);
 
 // Host: the FIR window taps[0..W) rearranged for the convolution kernel:
 // phase ph (0..D-1) holds, for t = 0, 1, ..., the tap w = W - 1 - (ph + t*D),
@@ -210,7 +214,6 @@ cudaError_t radix_sort_pairs(void* temp, size_t* temp_bytes, const uint32_t* key
 }  // namespace bcsim_gb300
 
 namespace bcsim_gb300 {
-// Reads and clears the device flag that a bounded wait sets when it gives up.
 // Scatterer ingestion (ingest.cu).  Spline control points [n][num_cs][3] ->
 // [num_cs][n] float4 (x, y, z, 0).
 cudaError_t launch_spline_transpose(const float* raw, int64_t n, int num_cs, float4* out, cudaStream_t stream);
@@ -225,7 +228,10 @@ cudaError_t abs_sum(const float* vals, int64_t stride, int64_t n, void* scratch,
 cudaError_t abs_sum_enqueue(const float* vals, int64_t stride, int64_t n, void* scratch, double* sum, int* nonfinite,
                             cudaStream_t stream);
 
-cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream);
+// A simulator's device error flag (SimParams::err_flag), which a kernel sets
+// when a bounded wait gives up: read it into *flag and clear it, synchronising
+// the stream.
+cudaError_t read_and_clear_error_flag(int* dev_flag, int* flag, cudaStream_t stream);
 // Copy of the error flag into host memory (pinned: asynchronous), in stream order.
-cudaError_t enqueue_error_flag_read(int* host_flag, cudaStream_t stream);
+cudaError_t enqueue_error_flag_read(const int* dev_flag, int* host_flag, cudaStream_t stream);
 }

@@ -12,7 +12,7 @@
 // device, and the host side uses only static buffers.
 //
 // Rules that come with a shared static array:
-//  * every GPU that loads this library holds the array (BCSIM_NOALLOC_SCRATCH_BYTES)
+//  * every GPU that loads this library holds the array (NA_TOTAL bytes, about 31.3 MiB)
 //    until the process exits;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call before
@@ -21,7 +21,15 @@
 //    are cleared at the start of every call, and calls whose work overlaps on the
 //    GPU (different streams, or different host threads) race on it -- serialise
 //    them on one stream;
-//  * sizes beyond the stated maxima are rejected with an error message.
+//  * sizes beyond the stated maxima are rejected with an error message;
+//  * the call is synchronous: it returns once the IQ is in the caller's buffer.
+//
+// The amplitudes are checked on the device before anything is projected: a
+// non-finite amplitude fails the call with the allocating path's message
+// ("Nan in scatterer projection."), and so does an amplitude_sum_bound below
+// the measured sum of |a| (the bound sets the fixed-point scale of the bins; an
+// understated one could overflow them).  That reduction keeps its partial sums
+// in its own region of the static array.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -51,7 +59,9 @@ constexpr size_t NA_PHOFF_OFF = NA_PM_OFF + (NA_MAX_TAPS + 4 * NA_MAX_DEC) * siz
 constexpr size_t NA_DEMOD_OFF = NA_PHOFF_OFF + 4096 * sizeof(int);
 static_assert(3 * NA_MAX_DEC + 1 <= 4096, "phase table fits its region");
 constexpr int NA_MAX_OUT = 65536;                                // decimated samples per line
-constexpr size_t NA_TOTAL = NA_DEMOD_OFF + NA_MAX_OUT * sizeof(float2);
+constexpr size_t NA_SUM_OFF = NA_DEMOD_OFF + NA_MAX_OUT * sizeof(float2);   // amplitude reduction
+constexpr size_t NA_SUM_BYTES = 8192;
+constexpr size_t NA_TOTAL = NA_SUM_OFF + NA_SUM_BYTES;
 constexpr int NA_MAX_FFT = 65536;                                // convolution length M
 
 static_assert(NA_TOTAL % 256 == 0, "scratch regions stay 256-byte aligned");
@@ -73,6 +83,8 @@ float2 g_demod[NA_MAX_OUT];
 LineGeom g_lines[NA_MAX_LINES];
 int g_ids[NA_MAX_LINES];
 LineTile g_tiles[NA_MAX_LINES];
+double g_amp_sum;
+int g_amp_nonfinite;
 
 void fft_inplace(std::complex<double>* x, int64_t n, int sign) {
     for (int64_t i = 1, j = 0; i < n; i++) {
@@ -120,7 +132,13 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
     if (radial_decimation < 1) return fail(err, err_cap, BCSIM_E_INVALID, "illegal radial decimation value");
     if (radial_decimation > NA_MAX_DEC)
         return fail(err, err_cap, BCSIM_E_CAPACITY, "radial decimation above 1024 for the allocation-free entry point");
-    if (sound_speed <= 0) return fail(err, err_cap, BCSIM_E_INVALID, "illegal sound speed");
+    if (!(sound_speed > 0) || !std::isfinite(sound_speed)) return fail(err, err_cap, BCSIM_E_INVALID, "illegal sound speed");
+    if (!(fs > 0) || !std::isfinite(fs)) return fail(err, err_cap, BCSIM_E_INVALID, "sampling frequency must be positive and finite");
+    if (!std::isfinite(line_length)) return fail(err, err_cap, BCSIM_E_INVALID, "line length must be finite");
+    if (!std::isfinite(demod_freq)) return fail(err, err_cap, BCSIM_E_INVALID, "demodulation frequency must be finite");
+    if (!(sigma_lateral > 0) || !std::isfinite(sigma_lateral) || !(sigma_elevational > 0) ||
+        !std::isfinite(sigma_elevational))
+        return fail(err, err_cap, BCSIM_E_INVALID, "beam sigmas must be positive and finite");
     if (num_taps < 1) return fail(err, err_cap, BCSIM_E_INVALID, "excitation has no samples");
     if (!(amplitude_sum_bound >= 0.0f) || !std::isfinite(amplitude_sum_bound))
         return fail(err, err_cap, BCSIM_E_INVALID, "amplitude_sum_bound must be a finite upper bound of sum |a|");
@@ -152,6 +170,41 @@ extern "C" int bcsim_simulate_fixed_noalloc(const void* d_xyza, int64_t n, const
     }
     unsigned char* base = static_cast<unsigned char*>(g_na_ptr[dev]);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the scatterers and the output must be device (or managed) memory of this
+    // device: a host pointer would fault inside the kernels
+    {
+        const void* ptrs[2] = {n > 0 ? d_xyza : nullptr, d_out};
+        const char* names[2] = {"d_xyza", "d_out"};
+        for (int k = 0; k < 2; k++) {
+            if (!ptrs[k]) continue;
+            cudaPointerAttributes at;
+            const cudaError_t pe = cudaPointerGetAttributes(&at, ptrs[k]);
+            if (pe != cudaSuccess) {
+                cudaGetLastError();
+                return fail(err, err_cap, BCSIM_E_INVALID, k == 0 ? "d_xyza is not a device pointer" : "d_out is not a device pointer");
+            }
+            const bool ok = at.type == cudaMemoryTypeManaged || (at.type == cudaMemoryTypeDevice && at.device == dev);
+            if (!ok) {
+                char msg[128];
+                std::snprintf(msg, sizeof msg, "%s is not device memory of the current device", names[k]);
+                return fail(err, err_cap, BCSIM_E_INVALID, msg);
+            }
+        }
+    }
+    // amplitudes: finite, and their sum of |a| within the caller's bound (the
+    // 0.1 % margin of the fixed-point scale below covers the bound's rounding
+    // to float); checked before anything is written
+    if (n > 0) {
+        if (abs_sum_scratch_bytes() > NA_SUM_BYTES)
+            return fail(err, err_cap, BCSIM_E_INTERNAL, "amplitude reduction scratch too small");
+        cudaError_t se = abs_sum_enqueue(static_cast<const float*>(d_xyza) + 3, 4, n, base + NA_SUM_OFF, &g_amp_sum,
+                                         &g_amp_nonfinite, st);
+        if (se == cudaSuccess) se = cudaStreamSynchronize(st);
+        if (se != cudaSuccess) return fail(err, err_cap, BCSIM_E_CUDA, cudaGetErrorString(se));
+        if (g_amp_nonfinite) return fail(err, err_cap, BCSIM_E_INVALID, "Nan in scatterer projection.");
+        if (g_amp_sum > (double)amplitude_sum_bound * 1.001)
+            return fail(err, err_cap, BCSIM_E_INVALID, "amplitude_sum_bound is below the sum of |amplitude| of the scatterers");
+    }
 
     // line table (elevational = lateral x direction, ScanSequence.cpp:40), identity order, tiles
     for (int i = 0; i < num_lines; i++) {

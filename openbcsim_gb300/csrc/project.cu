@@ -354,8 +354,6 @@ __global__ void gather_records_kernel(const uint32_t* __restrict__ svals, const 
 // ---------------------------------------------------------------------------
 // shared-origin projection
 // ---------------------------------------------------------------------------
-__device__ int g_bcsim_error_flag;   // set when a bounded wait gives up
-
 // The FP32 run sum of a line is folded into its integer bin total at absolute
 // record indices k * p.fold (128 or 512, fixed per configuration; chunks are
 // multiples of it), which bounds any FP32 summation to p.fold terms and keeps
@@ -467,11 +465,23 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         }
         __syncthreads();
     }
-    if (!mbar_wait(&bar, 0, 1u << 26)) {
-        g_bcsim_error_flag = 1;
-        mbar_wait(&bar, 0, 1u << 26);
+    // bounded wait for the records, decided once for the whole CTA: thread 0
+    // waits and publishes the outcome; if it gave up, the CTA sets the
+    // simulator's error flag and leaves together (thread 0 first waits once
+    // more, bounded, for the copy in flight).  Otherwise every thread observes
+    // the completed phase itself (at once), which orders the bulk copy's
+    // shared-memory writes before its reads.
+    __shared__ int s_gave_up;
+    if (tid == 0) s_gave_up = mbar_wait(&bar, 0, 1u << 26) ? 0 : 1;
+    __syncthreads();
+    if (s_gave_up) {
+        if (tid == 0) {
+            if (p.err_flag) atomicExch(p.err_flag, 1);
+            mbar_wait(&bar, 0, 1u << 26);
+        }
         return;
     }
+    mbar_wait(&bar, 0, 1u << 26);
 
     const int stride = PD ? 2 : 1;
     const float scale = p.scale;
@@ -1321,17 +1331,16 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
 #undef BCSIM_GEN
 }
 
-cudaError_t enqueue_error_flag_read(int* host_flag, cudaStream_t stream) {
-    return cudaMemcpyFromSymbolAsync(host_flag, g_bcsim_error_flag, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+cudaError_t enqueue_error_flag_read(const int* dev_flag, int* host_flag, cudaStream_t stream) {
+    return cudaMemcpyAsync(host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, stream);
 }
 
-cudaError_t read_and_clear_error_flag(int* flag, cudaStream_t stream) {
-    cudaError_t e = cudaMemcpyFromSymbolAsync(flag, g_bcsim_error_flag, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+cudaError_t read_and_clear_error_flag(int* dev_flag, int* flag, cudaStream_t stream) {
+    cudaError_t e = cudaMemcpyAsync(flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, stream);
     if (e != cudaSuccess) return e;
-    e = cudaStreamSynchronize(stream);
+    e = cudaMemsetAsync(dev_flag, 0, sizeof(int), stream);
     if (e != cudaSuccess) return e;
-    const int zero = 0;
-    return cudaMemcpyToSymbolAsync(g_bcsim_error_flag, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+    return cudaStreamSynchronize(stream);
 }
 
 cudaError_t radix_sort_pairs(void* temp, size_t* temp_bytes, const uint32_t* keys_in, uint32_t* keys_out,

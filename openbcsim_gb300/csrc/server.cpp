@@ -4,9 +4,19 @@
 // stay resident on the device.  A request asks for some scan lines of one
 // phantom (origins, directions, timestamps, line length, decimation).  One worker
 // thread admits queued requests in arrival order as soon as a simulator slot of
-// their phantom is free -- creating slots while the device-memory budget allows
-// -- prepares them on the host and enqueues their device work on the slot's own
-// stream, so requests that arrive while others are on the GPU overlap with them.
+// their phantom is free and the device memory the request needs is available --
+// creating slots while the budget allows -- prepares them on the host and
+// enqueues their device work on the slot's own stream, so requests that arrive
+// while others are on the GPU overlap with them.
+//
+// Admission by device memory: a request needs its slot's footprint for its
+// lines (bins, records, output); the growth beyond what the slot already holds
+// must fit in the memory available now -- the driver's free memory plus what
+// the device's stream-ordered pool holds reserved but unused (slots grow from
+// that pool) -- less a reserve.  A request that does not fit waits while others
+// are in flight (their completion can free slots for reuse); one that cannot
+// fit even with nothing in flight, or that exceeds the whole budget, fails with
+// BCSIM_E_MEMORY and the stream goes on.
 // The same thread polls completion events, hands each result (the pinned buffer
 // the device copied it to) to its request and records the submit-to-result
 // latency; the waiter copies it out.  Device buffers grow in stream order and
@@ -67,6 +77,7 @@ struct Slot {
     size_t bytes = 0;
     float2* host = nullptr;         // pinned staging for the result
     size_t host_bytes = 0;
+    int* flag = nullptr;            // pinned copy of the slot's device error flag, read with the result
     cudaEvent_t done = nullptr;
     std::shared_ptr<Request> req;
 };
@@ -101,11 +112,18 @@ struct bcsim_server {
     bool stop = false;
     std::thread worker;
     std::string last_error;
+    // host-side fault injection for tests (bcsim_server_debug_inject)
+    std::atomic<int> inject_wait_flag{0};     // raise the next admitted request's wait flag
+    std::atomic<int> inject_throw{0};         // make the next dispatch throw inside the worker
+    std::atomic<int64_t> free_cap{-1};        // cap on the available device memory admission sees
+    static constexpr size_t kReserve = (size_t)256 << 20;   // kept free for the driver and the pool's slack
 
     void run();
     bool dispatch(const std::shared_ptr<Request>& r);
     void poll();
     int busy_slots();
+    size_t available_memory();
+    void fail_request(const std::shared_ptr<Request>& r, int code, const std::string& msg);
 };
 
 namespace {
@@ -121,9 +139,42 @@ std::unique_ptr<Slot> make_slot(Simulator& base, size_t bytes) {
     const size_t pinned = (size_t)8 << 20;
     if (cudaMallocHost(&s->host, pinned) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
     s->host_bytes = pinned;
+    if (cudaMallocHost(&s->flag, sizeof(int)) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
+    *s->flag = 0;
     return s;
 }
 }  // namespace
+
+// Device memory a request can still take: the driver's free memory plus the
+// default pool's reserved-but-unused bytes (stream-ordered buffers are carved
+// from that pool, which keeps freed memory for reuse), less a reserve.
+size_t bcsim_server::available_memory() {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = 0;
+    }
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t reserved = 0, used = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+            free_b += (size_t)(reserved - used);
+    }
+    free_b = free_b > kReserve ? free_b - kReserve : 0;
+    const int64_t cap = free_cap.load();
+    if (cap >= 0 && (size_t)cap < free_b) free_b = (size_t)cap;
+    return free_b;
+}
+
+void bcsim_server::fail_request(const std::shared_ptr<Request>& r, int code, const std::string& msg) {
+    std::lock_guard<std::mutex> lock(mu);
+    r->done = true;
+    r->status = code;
+    r->error = msg;
+    failed++;
+    done_cv.notify_all();
+}
 
 int bcsim_server::busy_slots() {
     int n = 0;
@@ -139,16 +190,38 @@ bool bcsim_server::dispatch(const std::shared_ptr<Request>& r) {
     for (auto& s : ph.slots)
         if (!s->busy) { slot = s.get(); break; }
     const int64_t ns = ph.base->samples_for(r->line_length);
+    const size_t need = ph.base->footprint_bytes(r->num_lines, ns);
+    if (need > (size_t)budget) {
+        fail_request(r, BCSIM_E_MEMORY, "request needs " + std::to_string(need) + " bytes of device memory, above the "
+                                        "server's budget of " + std::to_string(budget));
+        return true;
+    }
+    // device memory this admission takes: a new slot's footprint, or the growth
+    // of a free slot's buffers
+    const size_t grow = slot ? (need > slot->bytes ? need - slot->bytes : 0) : need;
+    if (!slot && ((int)ph.slots.size() >= max_slots || (!ph.slots.empty() && in_use + (int64_t)need > budget)))
+        return false;   // wait for a slot of this phantom
+    if (grow > 0) {
+        const size_t avail = available_memory();
+        if (grow > avail) {
+            if (busy_slots() > 0) return false;   // completions may free slots to reuse
+            fail_request(r, BCSIM_E_MEMORY, "request needs " + std::to_string(grow) + " more bytes of device memory; " +
+                                            std::to_string(avail) + " available");
+            return true;
+        }
+    }
     if (!slot) {
-        const size_t need = ph.base->footprint_bytes(r->num_lines, ns);
-        if ((int)ph.slots.size() >= max_slots || (!ph.slots.empty() && in_use + (int64_t)need > budget)) return false;
         ph.slots.push_back(make_slot(*ph.base, need));
         in_use += (int64_t)need;
         slot = ph.slots.back().get();
+    } else if (need > slot->bytes) {
+        in_use += (int64_t)(need - slot->bytes);
+        slot->bytes = need;
     }
     slot->busy = true;
     slot->req = r;
     try {
+        if (inject_throw.exchange(0)) throw std::runtime_error("injected worker failure");
         Simulator& sim = *slot->sim;
         sim.set_parameter("radial_decimation", std::to_string(r->decimation));
         sim.set_scan_sequence(r->origins.data(), r->dirs.data(), r->lats.data(), r->ts.data(), r->num_lines,
@@ -158,17 +231,18 @@ bool bcsim_server::dispatch(const std::shared_ptr<Request>& r) {
         if (bytes > slot->host_bytes) {
             // pinned staging grows rarely (at least 8 MiB, then doubling): freeing
             // pinned memory can wait for the device
-            const size_t grow = std::max({bytes, slot->host_bytes * 2, (size_t)8 << 20});
+            const size_t grow_h = std::max({bytes, slot->host_bytes * 2, (size_t)8 << 20});
             if (slot->host) cudaFreeHost(slot->host);
             slot->host = nullptr;
             slot->host_bytes = 0;
-            if (cudaMallocHost(&slot->host, grow) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
-            slot->host_bytes = grow;
+            if (cudaMallocHost(&slot->host, grow_h) != cudaSuccess) throw SimError(BCSIM_E_MEMORY, "pinned host allocation failed");
+            slot->host_bytes = grow_h;
         }
         cudaStream_t st = sim.stream();
         sim.enqueue(st, sim.internal_output(), false);
+        if (inject_wait_flag.exchange(0)) sim.raise_device_flag();   // as a bounded wait that gave up would
         if (cudaMemcpyAsync(slot->host, sim.internal_output(), bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaEventRecord(slot->done, st) != cudaSuccess)
+            sim.enqueue_flag_read(slot->flag, st) != cudaSuccess || cudaEventRecord(slot->done, st) != cudaSuccess)
             throw SimError(BCSIM_E_CUDA, "enqueue failed");
         r->nd = sim.num_out_samples();
         r->projections = sim.total_num_scatterers() * (int64_t)r->num_lines;
@@ -193,8 +267,24 @@ void bcsim_server::poll() {
             const cudaError_t q = cudaEventQuery(s->done);
             if (q == cudaErrorNotReady) continue;
             std::shared_ptr<Request> r = s->req;
+            std::string flag_error;
+            if (q == cudaSuccess && *s->flag) {
+                // a bounded device wait of this request's kernels gave up: the
+                // result is incomplete (the check clears the slot's flag)
+                try {
+                    s->sim->check_device_flag();
+                } catch (const std::exception& e) {
+                    flag_error = e.what();
+                }
+                *s->flag = 0;
+                if (flag_error.empty()) flag_error = "a bounded device wait gave up; results are incomplete";
+            }
             std::lock_guard<std::mutex> lock(mu);
-            if (q == cudaSuccess) {
+            if (q == cudaSuccess && !flag_error.empty()) {
+                r->status = BCSIM_E_INTERNAL;
+                r->error = flag_error;
+                failed++;
+            } else if (q == cudaSuccess) {
                 // hand the staging buffer to the request; the slot takes a
                 // returned one (or allocates at its next dispatch)
                 r->iq = s->host;
@@ -320,6 +410,7 @@ int bcsim_server_destroy(bcsim_server* s) {
     for (int pi = 0; pi < s->num_phantoms.load(); pi++)
         for (auto& sl : s->phantoms[pi]->slots) {
             if (sl->host) cudaFreeHost(sl->host);
+            if (sl->flag) cudaFreeHost(sl->flag);
             if (sl->done) cudaEventDestroy(sl->done);
         }
     for (auto& b : s->free_pinned) cudaFreeHost(b.first);
@@ -433,6 +524,16 @@ int bcsim_server_wait(bcsim_server* s, int64_t request_id, float* out, int64_t c
         r->iq = nullptr;
     }
     return rc;
+}
+
+int bcsim_server_debug_inject(bcsim_server* s, int what, int64_t value) {
+    if (!s) return BCSIM_E_INVALID;
+    switch (what) {
+        case BCSIM_SERVER_INJECT_WAIT_FLAG: s->inject_wait_flag.store(1); return BCSIM_OK;
+        case BCSIM_SERVER_INJECT_WORKER_THROW: s->inject_throw.store(1); return BCSIM_OK;
+        case BCSIM_SERVER_INJECT_FREE_MEMORY_CAP: s->free_cap.store(value); return BCSIM_OK;
+        default: return BCSIM_E_INVALID;
+    }
 }
 
 int bcsim_server_stats(bcsim_server* s, int64_t* completed, int64_t* failed, double* p50_ms, double* p99_ms,

@@ -46,12 +46,37 @@ def gaussian_pulse_time_limit(fc: float, bw: float, bwr: float = -6.0, tpr: floa
                                       math.log(10.0 ** (bwr / 20.0))) * math.log10(math.e)))
 
 
+_LIBM = None
+
+
+def _libm():
+    """The C library's math (cosf, exp): the functions the reference's float
+    template calls, so that the taps come out bit for bit as its own."""
+    global _LIBM
+    if _LIBM is None:
+        import ctypes
+        import ctypes.util
+
+        try:
+            lib = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+            lib.cosf.restype, lib.cosf.argtypes = ctypes.c_float, [ctypes.c_float]
+            lib.exp.restype, lib.exp.argtypes = ctypes.c_double, [ctypes.c_double]
+            _LIBM = lib
+        except (OSError, AttributeError):
+            _LIBM = False
+    return _LIBM
+
+
 def gaussian_excitation(fc: float, bw: float, fs: float):
     """MakeGaussianExcitation<float> (GaussPulse.cpp:52-70).
 
     Returns (taps float32 [n], center_index).  The arithmetic follows the
-    reference's float/double mix so that the taps equal the reference's own to
-    within an ulp (the cosine is taken in double of the float argument).
+    reference's float/double mix: the time, the envelope's exponent numerator
+    and the cosine's argument in float, the exponent divided by a double
+    log(10^(-6/20)) and exponentiated in double, the cosine in float (the
+    float overload, the C library's cosf), their product rounded to float.
+    With the C library's cosf and exp the taps equal the reference's bit for
+    bit; without them (numpy's own functions) they may differ by an ulp.
     """
     fc32, bw32, fs32 = np.float32(fc), np.float32(bw), np.float32(fs)
     lim = gaussian_pulse_time_limit(float(fc32), float(bw32))
@@ -62,9 +87,15 @@ def gaussian_excitation(fc: float, bw: float, fs: float):
     f_cutoff = np.float32(bw32 * fc32)
     ftp = (f_cutoff * t).astype(np.float32)
     ppf = (((pi32 * pi32) * ftp).astype(np.float32) * ftp).astype(np.float32)
-    env = np.exp(ppf.astype(np.float64) / math.log(10.0 ** (-6.0 / 20.0)))
+    den = math.log(10.0 ** (-6.0 / 20.0))
     arg = (((np.float32(2) * pi32) * fc32).astype(np.float32) * t).astype(np.float32)
-    cos32 = np.cos(arg.astype(np.float64)).astype(np.float32)
+    lib = _libm()
+    if lib:
+        env = np.array([lib.exp(float(v) / den) for v in ppf], np.float64)
+        cos32 = np.array([lib.cosf(float(v)) for v in arg], np.float32)
+    else:
+        env = np.exp(ppf.astype(np.float64) / den)
+        cos32 = np.cos(arg.astype(np.float64)).astype(np.float32)
     taps = (env * cos32.astype(np.float64)).astype(np.float32)
     return taps, n // 2
 
@@ -264,6 +295,9 @@ class Job:
     sound_speed: float = SOUND_SPEED
     phase_delay: bool = True
     arc: bool = True
+    noise_amplitude: float = 0.0   # sigma of the seeded complex noise on the time projection (0: off)
+    noise_seed: int = 0
+    noise_frame: int = 0           # the frame number the noise is drawn for
 
     @property
     def num_scatterers(self) -> int:

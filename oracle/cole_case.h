@@ -70,6 +70,12 @@ typedef struct {
     /* spline scatterer datasets */
     int                    num_spline_sets;
     const cole_spline_set* spline_sets;
+    /* seeded complex noise N(0, noise_sigma) on every time-projection sample
+     * j < ns (noise_amplitude, CpuAlgorithm.cpp:340-347), keyed by (noise_seed,
+     * noise_frame, line, j); 0 = off.  Not read by the reference driver. */
+    float        noise_sigma;
+    uint64_t     noise_seed;
+    uint32_t     noise_frame;
 } cole_case;
 
 #ifdef __cplusplus

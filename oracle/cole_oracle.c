@@ -490,6 +490,33 @@ static int project_line(const ctx_t* x, int line_no, double* wr, double* wi, flo
     return ORACLE_OK;
 }
 
+/* Philox4x32-10 (Salmon, Moraes, Dror and Shaw, SC 2011): ten rounds of two
+ * 32x32->64 multiplications, the key bumped by the Weyl constants between rounds. */
+static void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; r++) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        c[0] = n0; c[1] = (uint32_t)p1; c[2] = n2; c[3] = (uint32_t)p0;
+    }
+}
+
+/* The Philox block itself, for known-answer tests. */
+void oracle_philox4x32_10(uint32_t* c, uint32_t k0, uint32_t k1) { philox4x32_10(c, k0, k1); }
+
+/* Unit-variance noise (re, im) of sample j of line `line` in frame `frame`:
+ * Philox block of counter (j, line, frame, 0x6e6f6973) under the 64-bit seed;
+ * Box-Muller of u1 = (w0 >> 8 + 1/2) 2^-24 and u2 = (w1 >> 8) 2^-24, in double. */
+void oracle_bin_noise(uint64_t seed, uint32_t frame, int line, int64_t j, double* re, double* im) {
+    uint32_t c[4] = {(uint32_t)j, (uint32_t)line, frame, 0x6e6f6973u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u1 = ((double)(c[0] >> 8) + 0.5) * 0x1p-24;
+    const double u2 = (double)(c[1] >> 8) * 0x1p-24;
+    const double rad = sqrt(-2.0 * log(u1));
+    *re = rad * cos(TWO_PI_D * u2);
+    *im = rad * sin(TWO_PI_D * u2);
+}
+
 static int simulate_one_line(const ctx_t* x, int line_no, double* wr, double* wi, float* fr, float* fi,
                              float* out, char* err, int errcap) {
     const cole_case* c = x->c;
@@ -512,6 +539,15 @@ static int simulate_one_line(const ctx_t* x, int line_no, double* wr, double* wi
                 snprintf(err, (size_t)errcap, "Nan in scatterer projection.");
                 return ORACLE_ERR;
             }
+        }
+    }
+    /* Gaussian noise on the time projection (CpuAlgorithm.cpp:340-347), seeded */
+    if (c->noise_sigma > 0.0f) {
+        for (int64_t i = 0; i < ns; i++) {
+            double nr, ni;
+            oracle_bin_noise(c->noise_seed, c->noise_frame, line_no, i, &nr, &ni);
+            wr[i] += (double)c->noise_sigma * nr;
+            wi[i] += (double)c->noise_sigma * ni;
         }
     }
 

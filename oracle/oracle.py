@@ -48,7 +48,19 @@ class CaseC(C.Structure):
                 ("origins", _f32p), ("directions", _f32p), ("lateral_dirs", _f32p), ("timestamps", _f32p),
                 ("num_fixed_sets", C.c_int), ("fixed_counts", C.POINTER(C.c_int64)),
                 ("fixed_xyza", C.POINTER(_f32p)),
-                ("num_spline_sets", C.c_int), ("spline_sets", C.POINTER(SplineSetC))]
+                ("num_spline_sets", C.c_int), ("spline_sets", C.POINTER(SplineSetC)),
+                ("noise_sigma", C.c_float), ("noise_seed", C.c_uint64), ("noise_frame", C.c_uint32)]
+
+
+def reference_sources() -> str:
+    """Where the reference's source tree is read from: $BCSIM_REF_SRC, else the
+    default of oracle/Makefile (the recipe that compiles it).  The directory may
+    be absent (then the reference-backed checks are skipped)."""
+    env = os.environ.get("BCSIM_REF_SRC")
+    if env:
+        return env
+    out = subprocess.run(["make", "-s", "-C", HERE, "print-ref-src"], capture_output=True, text=True)
+    return out.stdout.strip()
 
 
 def build(quiet: bool = True) -> None:
@@ -99,6 +111,11 @@ def oracle_lib():
     lib.oracle_project_bins.argtypes = [C.POINTER(CaseC), C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int64, C.c_char_p, C.c_int]
     lib.oracle_project_bins.restype = C.c_int
     lib.oracle_analytic_spectrum.argtypes = [_f32p, C.c_int, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.oracle_bin_noise.argtypes = [C.c_uint64, C.c_uint32, C.c_int, C.c_int64, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
+    lib.oracle_bin_noise.restype = None
+    lib.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.c_uint32, C.c_uint32]
+    lib.oracle_philox4x32_10.restype = None
     return lib
 
 
@@ -181,6 +198,9 @@ class Case:
             sets[i].control_points, sets[i].amplitudes = fptr(cp), fptr(am)
         self.keep.append(sets)
         c.num_spline_sets, c.spline_sets = ns, sets
+        c.noise_sigma = float(getattr(job, "noise_amplitude", 0.0))
+        c.noise_seed = int(getattr(job, "noise_seed", 0))
+        c.noise_frame = int(getattr(job, "noise_frame", 0))
         self.c = c
 
 
@@ -213,6 +233,17 @@ def ref_simulate(job, threads: int = 0) -> np.ndarray:
                           C.byref(nl), C.byref(nsmp), err, 512)
     if rc != 0:
         raise RuntimeError(err.value.decode())
+    return out
+
+
+def bin_noise(seed: int, frame: int, line: int, count: int) -> np.ndarray:
+    """Unit-variance seeded noise of samples 0..count-1 of one line: complex128 [count]."""
+    lib = oracle_lib()
+    out = np.empty(count, np.complex128)
+    re, im = C.c_double(), C.c_double()
+    for j in range(count):
+        lib.oracle_bin_noise(seed, frame, line, j, C.byref(re), C.byref(im))
+        out[j] = complex(re.value, im.value)
     return out
 
 

@@ -9,6 +9,10 @@
   (sector, tilted sector, linear) and what the reference's own scan converter
   (CpuCartesianator, src/utils/cartesianator/Cartesianator.cpp:107-205)
   returns for them.
+* ref_excitation.npz -- the taps and centre index that the reference's own
+  MakeGaussianExcitation<float> (src/utils/GaussPulse.cpp:52-70) returns for
+  the pulses of the benchmark workloads and a spread of others
+  (`python tests/golden/make_golden.py excitation`).
 * ref_<case>.npz -- inputs of a small seeded case, the IQ that the reference's
   own CPU algorithm returns for them (bcsim::Create("cpu")->simulate_lines), and
   the time-projection bins of a few lines from its projection loops
@@ -169,6 +173,26 @@ def make_imaging():
     print("imaging", os.path.getsize(os.path.join(HERE, "ref_imaging.npz")))
 
 
+# (centre frequency, fractional bandwidth, sampling frequency): the workloads'
+# pulses (2.5 MHz / 0.1, 3.5 MHz / 0.15 at 50 MHz), the batch range's corners
+# (2-7 MHz, 0.1-0.3) and other sampling rates
+EXCITATIONS = [(2.5e6, 0.1, 50e6), (3.5e6, 0.15, 50e6), (2e6, 0.1, 50e6), (7e6, 0.3, 50e6), (2e6, 0.3, 50e6),
+               (7e6, 0.1, 50e6), (4.37e6, 0.213, 50e6), (5e6, 0.5, 100e6), (1e6, 0.05, 20e6), (10e6, 0.6, 80e6)]
+
+
+def make_excitation():
+    lib = O.ref_lib()
+    d = {"params": np.array(EXCITATIONS, np.float64)}
+    for k, (fc, bw, fs) in enumerate(EXCITATIONS):
+        buf = np.zeros(1 << 16, np.float32)
+        ci = O.C.c_int()
+        n = lib.ref_gaussian_excitation(fc, bw, fs, O.fptr(buf), buf.size, O.C.byref(ci))
+        d[f"taps_{k}"] = buf[:n].copy()
+        d[f"center_{k}"] = np.array(ci.value)
+    np.savez_compressed(os.path.join(HERE, "ref_excitation.npz"), **d)
+    print("excitation", os.path.getsize(os.path.join(HERE, "ref_excitation.npz")))
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libbcsim_ref.so is missing: run `make -C oracle all` where the reference sources are")
@@ -188,6 +212,9 @@ def main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["imaging"]:
         make_imaging()
+    elif sys.argv[1:] == ["excitation"]:
+        make_excitation()
     else:
         main()
         make_imaging()
+        make_excitation()

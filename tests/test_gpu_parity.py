@@ -224,18 +224,84 @@ def test_spline_time_outside_knots():
         run(job)
 
 
+def _line_subset(job, idx):
+    """The job restricted to scan lines idx (lines are independent)."""
+    import copy
+
+    from openbcsim_gb300 import workloads as W
+
+    sub = copy.copy(job)
+    s = job.scan
+    sub.scan = W.ScanSequence(s.origins[idx], s.directions[idx], s.lateral_dirs[idx], s.timestamps[idx],
+                              s.line_length)
+    return sub
+
+
+def _spread_lines(which, L):
+    if which == "sector_2d_fixed":
+        return np.arange(L)                                   # the whole frame
+    if which == "sector_spline":
+        return np.unique(np.linspace(0, L - 1, 128).round().astype(int))
+    # 64 x 64 volume: a spread of 256 lines over the grid (its stride is not a
+    # multiple of the row length, so azimuths vary), the four corners, the
+    # middles of the four edges and the centre lines
+    n = int(round(np.sqrt(L)))
+    extra = [0, n - 1, L - n, L - 1, n // 2, L - n + n // 2, (n // 2) * n, (n // 2) * n + n - 1,
+             (n // 2) * n + n // 2 - 1, (n // 2) * n + n // 2]
+    return np.unique(np.concatenate([np.linspace(0, L - 1, 256).round().astype(int), extra]))
+
+
 @pytest.mark.parametrize("which", ["sector_2d_fixed", "volume_3d_lut", "sector_spline"])
-def test_full_size_lines_vs_oracle(oracle, which):
-    """The workloads at full size; a few lines checked against the FP64 oracle."""
+def test_full_size_frames_vs_oracle(oracle, which):
+    """The workloads at full size against the FP64 oracle: every line of the
+    2-D sector frame (128), 128 lines spread over the spline frame's 1024, and
+    256 spread lines of the 64 x 64 volume plus its corners, edge middles and
+    centre; each over all its samples."""
     from openbcsim_gb300 import workloads as W
 
     job = getattr(W, which)()
     iq = run(job)
     assert np.isfinite(iq).all()
-    L = job.scan.num_lines
-    for lo in (0, L // 2 - 2, L - 4):
-        ref = oracle.simulate(job, oracle.MODE_FP64, line_begin=lo, line_end=lo + 4)
-        assert oracle.rel_rms(iq[lo:lo + 4], ref) <= FP64_TOL, (which, lo)
+    idx = _spread_lines(which, job.scan.num_lines)
+    ref = oracle.simulate(_line_subset(job, idx), oracle.MODE_FP64)
+    assert oracle.rel_rms(iq[idx], ref) <= FP64_TOL, which
+    # and no line is off on its own: the worst line's relative RMS
+    worst = max(oracle.rel_rms(iq[i], ref[k]) for k, i in enumerate(idx) if np.abs(ref[k]).max() > 0)
+    assert worst <= 10 * FP64_TOL, (which, worst)
+
+
+def test_render_once_at_shared_timestamp(oracle):
+    """Splines that every line sees at one timestamp from one origin are
+    rendered once into shared-origin records (the reference renders them to
+    fixed scatterers first, GpuAlgorithm.cpp:181-187 and
+    GpuScatterers.cpp:48-123), alone and mixed with fixed scatterers: the frame
+    matches the FP64 oracle, the per-pair evaluation of the same splines
+    (render_once=off) and, in reference arithmetic, the oracle's REF32 mode."""
+    from openbcsim_gb300 import workloads as W
+
+    rng = np.random.default_rng(81)
+    sp = W.random_spline(rng, 40_000, 16)
+    fixed = W.random_fixed(rng, 20_000, (-0.03, 0.03), None, (0.01, 0.12))
+    scan = W.sector_scan(96, 35.0, 0.12, timestamps=np.full(96, 0.37, np.float32))
+    for fixed_sets in ([], [fixed]):
+        job = W._excitation_job("render_once", scan, 2.5e6, 0.1, W.GaussianBeam(1e-3, 1e-3), fixed_sets, [sp], 10)
+        sim = engine(job, store_kernel_details="on")
+        once = sim.simulate_lines_line_major().copy()
+        # the shared-origin path ran (its record preparation was timed)
+        assert len(sim.get_debug_data("prep_sort_ms")) == 1
+        per_pair_sim = engine(job, store_kernel_details="on", render_once="off")
+        per_pair = per_pair_sim.simulate_lines_line_major().copy()
+        if not fixed_sets:
+            with pytest.raises(RuntimeError):
+                per_pair_sim.get_debug_data("prep_sort_ms")   # no shared-origin records at all
+        ref = oracle.simulate(job, oracle.MODE_FP64)
+        assert oracle.rel_rms(once, ref) <= FP64_TOL
+        assert oracle.rel_rms(per_pair, ref) <= FP64_TOL
+        assert oracle.rel_rms(once, per_pair) <= 3e-5
+        # deterministic, and bit-identical when simulated again
+        assert np.array_equal(once, sim.simulate_lines_line_major())
+        ref32 = oracle.simulate(job, oracle.MODE_REF32)
+        assert oracle.rel_rms(run(job, "reference"), ref32) <= REF32_TOL
 
 
 def test_large_phantom_few_lines(oracle):

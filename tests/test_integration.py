@@ -1,21 +1,21 @@
-"""The C++ IAlgorithm adapter of INTEGRATION.md compiles against the
-reference's own headers and links against the engine (where the reference
-sources are present; nothing here needs a GPU)."""
+"""The C++ IAlgorithm adapter (openbcsim_gb300/adapter/GB300Algorithm.hpp)
+compiles against the reference's own headers and links against the engine
+(where the reference sources are present; nothing here needs a GPU)."""
 import os
-import re
 import subprocess
 
 import pytest
 
 from conftest import ROOT
+from oracle.oracle import reference_sources
 
-REF = "/root/reference/src"
+REF = reference_sources()
+ADAPTER = os.path.join(ROOT, "openbcsim_gb300", "adapter", "GB300Algorithm.hpp")
 
 
 def adapter_source():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```cpp\n(.*?)```", text, re.S)
-    return next(b for b in blocks if "class GB300Algorithm" in b)
+    with open(ADAPTER) as f:
+        return f.read()
 
 
 MAIN = r'''
@@ -33,7 +33,7 @@ int main() {
 '''
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(REF), reason="reference sources not present")
 def test_adapter_compiles_links_and_reports_errors(tmp_path):
     from openbcsim_gb300 import build
 

@@ -87,3 +87,39 @@ def test_gaussian_excitation_matches_restatement(oracle):
         taps, c = W.gaussian_excitation(fc, bw, 50e6)
         assert n == len(taps) and ci.value == c
         np.testing.assert_allclose(buf[:n], taps, rtol=0, atol=2e-7)
+
+
+def _excitation_fixture():
+    import os
+
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "ref_excitation.npz"))
+    return [(tuple(p), z[f"taps_{k}"], int(z[f"center_{k}"])) for k, p in enumerate(z["params"])]
+
+
+def test_gaussian_excitation_pinned_to_reference():
+    """The package's pulse generator against the taps that the reference's own
+    MakeGaussianExcitation<float> (src/utils/GaussPulse.cpp:52-70, compiled by
+    oracle/Makefile) returned for ten pulses (tests/golden/ref_excitation.npz):
+    the same length and centre index and the same taps, bit for bit (the
+    generator calls the C library's cosf and exp, as the reference does)."""
+    from openbcsim_gb300 import workloads as W
+
+    for (fc, bw, fs), ref_taps, ref_center in _excitation_fixture():
+        taps, center = W.gaussian_excitation(fc, bw, fs)
+        assert len(taps) == len(ref_taps) and center == ref_center, (fc, bw, fs)
+        assert np.array_equal(taps, ref_taps), (fc, bw, fs)
+
+
+def test_gaussian_excitation_live_reference(oracle):
+    """Where the reference is compiled here, it still gives the fixture's taps."""
+    if not oracle.ref_available():
+        pytest.skip("reference not compiled on this machine")
+    lib = oracle.ref_lib()
+    for (fc, bw, fs), ref_taps, ref_center in _excitation_fixture():
+        buf = np.zeros(1 << 16, np.float32)
+        ci = C.c_int()
+        n = lib.ref_gaussian_excitation(fc, bw, fs, buf.ctypes.data_as(C.POINTER(C.c_float)), buf.size, C.byref(ci))
+        assert n == len(ref_taps) and ci.value == ref_center
+        assert np.array_equal(buf[:n], ref_taps)
