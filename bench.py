@@ -69,8 +69,12 @@ def flops_per_projection(lut: bool, phase_delay: bool, spline_degree=None) -> fl
 
 def make_job(name: str, num_scatterers: int = 0, lines: str = ""):
     """The named workload, optionally with fewer scatterers / lines (for
-    profiling captures on a small case)."""
+    profiling captures on a small case); "batch_uneven:J" is job J of the
+    64-job batch workload."""
     from openbcsim_gb300 import workloads as W
+
+    if name.startswith("batch_uneven:"):
+        return W.batch_uneven()[int(name.split(":", 1)[1])]
 
     kw = {}
     if num_scatterers:

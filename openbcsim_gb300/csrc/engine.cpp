@@ -1083,6 +1083,11 @@ void Simulator::prepare() {
         g.d = d;
         g.tile_off = all_tiles.size();
         g.num_tiles = tiles.size();
+        // CTAs as wide as the widest tile: a job of fewer lines than a full tile
+        // launches no warps without lines
+        int most = 1;
+        for (const auto& t : tiles) most = std::max(most, t.count);
+        g.threads = std::min(PAIR_THREADS, (most + 31) / 32 * 32);
         g.basis_off = all_basis.size();
         const size_t id_off = all_ids.size();
         if (P.tile_cull)
@@ -1277,7 +1282,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                                   R.vals_out.as<uint32_t>(), R.counts.as<int>(), 0, lines_d,
                                                   gen_line_ids_.as<int>(), gen_tiles_.as<LineTile>() + g.tile_off,
                                                   (int)g.num_tiles, nullptr, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
-                                                  pair_counts));
+                                                  pair_counts, g.threads));
             } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
                 ++launches;
@@ -1286,7 +1291,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                                   gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
-                                                  pair_counts));
+                                                  pair_counts, g.threads));
             }
         }
         if (timing) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
@@ -1303,7 +1308,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                               nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles, nullptr, p,
                                               b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
-                                                  pair_counts));
+                                                  pair_counts, g.threads));
         } else {
             if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
@@ -1312,7 +1317,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                               gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
-                                                  pair_counts));
+                                                  pair_counts, g.threads));
         }
     }
     if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
@@ -1415,40 +1420,55 @@ void Simulator::raise_device_flag() {
     BCSIM_CUDA(cudaStreamSynchronize(stream_));
 }
 
-// Lines-per-tile and records-per-CTA from measurement: every candidate launch
-// shape is timed on this configuration once and the fastest is kept, per shape
-// class (path, beam, phase delay, scatterer and line count buckets).  Tile
-// shapes never change the results (fixed-point sums; FP32 partial sums are
+// Launch shapes from measurement, per shape class (path, beam, phase delay,
+// scatterer and line count buckets, spline degree): the per-pair projection's
+// lines per tile {128, 96, 64}, then the shared-origin kernel's scatterers
+// (records) per CTA {128 ... 1024}; each candidate timed on this
+// configuration (best of two) and the fastest kept.  No shape changes the results (fixed-point sums; FP32 partial sums
 // aligned to absolute record indices), only the time.
 void Simulator::autotune() {
-    Plan& P = plan_;
+    if (autotuning_) return;
     auto bucket = [](int64_t v) { int b = 0; while (v > 1) { v >>= 1; b++; } return b; };
+    bool has_pair = false;
+    for (const GenLaunch& g : plan_.gl)
+        has_pair = has_pair || (g.kind == 0 ? !plan_.shared : !plan_.spline_shared[g.d]);
     const int64_t n_pairs = total_num_scatterers();
-    const std::string key = std::to_string(P.shared) + "/" + std::to_string(beam_type_) + "/" +
+    const std::string key = std::to_string(plan_.shared) + "/" + std::to_string(beam_type_) + "/" +
                             std::to_string(phase_delay_) + "/" + std::to_string(bucket(n_pairs)) + "/" +
-                            std::to_string(bucket(num_lines_)) + "/" + std::to_string(splines_.empty());
+                            std::to_string(bucket(num_lines_)) + "/" +
+                            std::to_string(splines_.empty() ? -1 : splines_[0].degree) + "/" +
+                            std::to_string(has_pair);
+    struct Tuned {
+        int chunk, tile_lines;
+    };
     static std::mutex mtx;
-    static std::map<std::string, std::pair<int, int>> cache;   // key -> (chunk, tile lines)
+    static std::map<std::string, Tuned> cache;
+    struct Guard {
+        bool& f;
+        explicit Guard(bool& x) : f(x) { f = true; }
+        ~Guard() { f = false; }
+    } guard(autotuning_);
+    auto replan = [&](int tl) {
+        tile_lines_ = tl;
+        plan_.version = ~0ull;   // rebuild the tiles for the new line count
+        prepare();
+    };
     {
         std::lock_guard<std::mutex> lock(mtx);
         auto it = cache.find(key);
         if (it != cache.end()) {
-            if (P.n_shared > 0) P.chunk = it->second.first;
+            const Tuned t = it->second;
+            if (t.tile_lines != tile_lines_) replan(t.tile_lines);
+            if (plan_.n_shared > 0) plan_.chunk = t.chunk;
             return;
         }
     }
-    std::vector<int> chunks = {P.chunk};
-    if (P.n_shared > 0) chunks = P.p.fold == 512 ? std::vector<int>{512, 1024} : std::vector<int>{128, 256, 512, 1024};
     const cudaStream_t st = stream_;
     out_.reserve((size_t)num_lines_ * nd_ * sizeof(float2), stream_);
     cudaEvent_t e0, e1;
     BCSIM_CUDA(cudaEventCreate(&e0));
     BCSIM_CUDA(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int best_chunk = P.chunk;
-    enqueue(st, out_.as<float2>(), false);   // records, warm-up
-    for (int c : chunks) {
-        P.chunk = c;
+    auto time_it = [&]() {
         float ms_min = 1e30f;
         for (int rep = 0; rep < 2; rep++) {
             BCSIM_CUDA(cudaEventRecord(e0, st));
@@ -1459,14 +1479,37 @@ void Simulator::autotune() {
             BCSIM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             ms_min = std::min(ms_min, ms);
         }
-        if (ms_min < best) { best = ms_min; best_chunk = c; }
+        return ms_min;
+    };
+    Tuned best{plan_.chunk, tile_lines_};
+    float best_ms = 1e30f;
+    enqueue(st, out_.as<float2>(), false);   // records, warm-up
+    if (has_pair) {
+        for (int tl : {0, 96, 64}) {
+            if (tl != tile_lines_) replan(tl);
+            enqueue(st, out_.as<float2>(), false);
+            const float ms = time_it();
+            if (ms < best_ms) { best_ms = ms; best = Tuned{plan_.chunk, tl}; }
+        }
+        if (best.tile_lines != tile_lines_) replan(best.tile_lines);
+    }
+    if (plan_.n_shared > 0) {
+        const std::vector<int> chunks = plan_.p.fold == 512 ? std::vector<int>{512, 1024}
+                                                            : std::vector<int>{128, 256, 512, 1024};
+        best_ms = 1e30f;
+        for (int c : chunks) {
+            plan_.chunk = c;
+            const float ms = time_it();
+            if (ms < best_ms) { best_ms = ms; best.chunk = c; }
+        }
+        plan_.chunk = best.chunk;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    P.chunk = best_chunk;
     std::lock_guard<std::mutex> lock(mtx);
-    cache[key] = {best_chunk, 0};
-    log(0, "autotune " + key + ": records per CTA " + std::to_string(best_chunk));
+    cache[key] = best;
+    log(0, "autotune " + key + ": records per CTA " + std::to_string(best.chunk) + ", lines per tile " +
+               std::to_string(best.tile_lines));
 }
 
 void Simulator::simulate_host(float* host_out, int64_t cap_complex, int64_t* lines, int64_t* samples) {

@@ -114,6 +114,7 @@ struct GenLaunch {
     int kind;
     int d;
     size_t tile_off, num_tiles, basis_off;
+    int threads;   // CTA size: the largest tile's line count rounded up to warps
 };
 
 // Host-side plan of one configuration: launch constants and shapes, built by
@@ -293,6 +294,7 @@ private:
     bool render_once_ = true;
     bool record_cache_ = true;   // reuse the sorted shared-origin records while their inputs are unchanged
     bool autotune_ = false;
+    bool autotuning_ = false;    // inside autotune(): its own re-plans do not tune again
     bool wide_cta_ = true;       // shared-origin kernel launch shape (see launch_project_shared)
     bool lut_smem_ = true;       // wide shared-origin kernel: stage the chunk's lookup-table planes in shared memory
     bool count_pairs_ = false;   // instrumented shared-origin kernel: visited / non-zero (record, line) pairs

@@ -158,13 +158,15 @@ cudaError_t launch_project_shared(const float4* records, int64_t plane, const in
 // culling), a scatterer that no line of a tile can see with a contribution
 // that survives the fixed-point rounding is left out of that tile.  pair_counts
 // (normally null): pair_counts[3] += the (scatterer, line) pairs evaluated.
+// threads: the CTA size, a multiple of 32 no smaller than any tile's line
+// count and at most PAIR_THREADS.
 cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const float* amps, int64_t n,
                                    int num_cs, int degree, const uint32_t* index_list, const int* counts,
                                    int64_t list_lo,
                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles,
                                    int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
                                    unsigned long long* bins, cudaStream_t stream, const TileBox* boxes = nullptr,
-                                   unsigned long long* pair_counts = nullptr);
+                                   unsigned long long* pair_counts = nullptr, int threads = PAIR_THREADS);
 
 // Fused convolution with the analytic pulse (direct FIR over a tap window),
 // IQ demodulation and radial decimation, from fixed-point bins to complex64.

@@ -830,8 +830,8 @@ __device__ __forceinline__ bool pair_bin(df dx, df dy, df dz, float dot, const S
 // (or lies outside the lookup table by a margin) is skipped -- exactly, since it
 // would add 0 -- and only the remaining pairs compute the float-pair time of
 // flight and add their contribution with integer atomics.
-template <int BEAM, bool SPLINE, bool REF>
-__global__ void __launch_bounds__(PAIR_THREADS)
+template <int BEAM, bool SPLINE, bool REF, int DEG>
+__global__ void __launch_bounds__(PAIR_THREADS, (SPLINE && DEG >= 0) ? 6 : 0)
     project_generic_kernel(const float4* __restrict__ xyza, const float4* __restrict__ cps,
                            const float* __restrict__ amps, int64_t n, int degree,
                            const uint32_t* __restrict__ index_list, const int* __restrict__ counts,
@@ -855,7 +855,11 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         count = __ldg(counts + 1);
     }
     const int tid = threadIdx.x;
-    const int np = degree + 1;
+    // non-zero basis functions per line: DEG + 1 for a spline degree fixed at
+    // compile time (the cubic case: fewer registers, six CTAs per SM), else the
+    // runtime degree's
+    constexpr int NB = DEG >= 0 ? DEG + 1 : MAX_SPLINE_DEGREE + 1;
+    const int np = DEG >= 0 ? DEG + 1 : degree + 1;
     // control points staged per scatterer, and scatterers per chunk so that
     // they fit the shared array
     const int span = SPLINE ? tile.span : 1;
@@ -867,16 +871,13 @@ __global__ void __launch_bounds__(PAIR_THREADS)
     const float rx = __ldg(&g->d[0]), ry = __ldg(&g->d[1]), rz = __ldg(&g->d[2]);
     const float lx = __ldg(&g->l[0]), ly = __ldg(&g->l[1]), lz = __ldg(&g->l[2]);
     const float ex = __ldg(&g->e[0]), ey = __ldg(&g->e[1]), ez = __ldg(&g->e[2]);
-    float bh[MAX_SPLINE_DEGREE + 1], bl[MAX_SPLINE_DEGREE + 1];
+    float bh[NB];   // the line's basis (high parts; the low parts are read at rounding ties only)
     int win = 0;   // this line's first control point within the staged window
     if (SPLINE) {
         const LineBasis* lb = basis + line;
         win = __ldg(&lb->mu) - tile.mu;
 #pragma unroll
-        for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
-            bh[k] = k < np ? __ldg(&lb->hi[k]) : 0.0f;
-            bl[k] = k < np ? __ldg(&lb->lo[k]) : 0.0f;
-        }
+        for (int k = 0; k < NB; k++) bh[k] = k < np ? __ldg(&lb->hi[k]) : 0.0f;
     }
     const int stride = p.phase_delay ? 2 : 1;
     unsigned long long* lbins = bins + (int64_t)line * p.ns * stride;
@@ -999,7 +1000,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                 // the basis sums to one: P = R + sum_k B_k (C_k - R)
                 R = sr[i];
 #pragma unroll
-                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                for (int k = 0; k < NB; k++) {
                     if (k < np) {
                         const float4 c = sp[i * span + win + k];
                         Sx = fmaf(bh[k], c.x, Sx); Sy = fmaf(bh[k], c.y, Sy); Sz = fmaf(bh[k], c.z, Sz);
@@ -1048,16 +1049,18 @@ __global__ void __launch_bounds__(PAIR_THREADS)
                 df sx = df_make(0.f, 0.f), sy = df_make(0.f, 0.f), sz = df_make(0.f, 0.f);
                 float ex_ = 0.f, ey_ = 0.f, ez_ = 0.f;   // accumulated low parts
                 const int gs = sidx[i];
+                const LineBasis* lbs = basis + line;
 #pragma unroll
-                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                for (int k = 0; k < NB; k++) {
                     if (k < np) {
                         const float4 c = __ldg(cps + (int64_t)(tile.mu - degree + win + k) * n + gs);
+                        const float blk = __ldg(&lbs->lo[k]);
                         const df px = two_prod(bh[k], c.x), py = two_prod(bh[k], c.y), pz = two_prod(bh[k], c.z);
                         const df tx = two_sum(sx.hi, px.hi), ty = two_sum(sy.hi, py.hi), tz = two_sum(sz.hi, pz.hi);
                         sx.hi = tx.hi; sy.hi = ty.hi; sz.hi = tz.hi;
-                        ex_ += tx.lo + fmaf(bl[k], c.x, px.lo);
-                        ey_ += ty.lo + fmaf(bl[k], c.y, py.lo);
-                        ez_ += tz.lo + fmaf(bl[k], c.z, pz.lo);
+                        ex_ += tx.lo + fmaf(blk, c.x, px.lo);
+                        ey_ += ty.lo + fmaf(blk, c.y, py.lo);
+                        ez_ += tz.lo + fmaf(blk, c.z, pz.lo);
                     }
                 }
                 const df ux = two_sum(sx.hi, -ox), uy = two_sum(sy.hi, -oy), uz = two_sum(sz.hi, -oz);
@@ -1125,7 +1128,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
             if (SPLINE) {
                 float sx = 0.f, sy = 0.f, sz = 0.f;
 #pragma unroll
-                for (int k = 0; k <= MAX_SPLINE_DEGREE; k++) {
+                for (int k = 0; k < NB; k++) {
                     if (k < np) {
                         const float4 c = sp[i * span + win + k];
                         sx = __fadd_rn(sx, __fmul_rn(c.x, bh[k]));
@@ -1292,20 +1295,21 @@ cudaError_t launch_project_shared(const float4* records, int64_t plane, const in
 #undef BCSIM_SH
 }
 
-template <int BEAM, bool SPLINE, bool REF>
+template <int BEAM, bool SPLINE, bool REF, int DEG>
 static cudaError_t launch_generic_t(const float4* xyza, const float4* cps, const float* amps, int64_t n, int degree,
                                     const uint32_t* index_list, const int* counts, int64_t list_lo,
                                     const LineGeom* lines, const int* line_ids, const LineTile* tiles,
                                     int num_tiles, const LineBasis* basis, const SimParams& p, const BeamDev& b,
                                     unsigned long long* bins, cudaStream_t stream, const TileBox* boxes,
-                                    unsigned long long* pair_counts) {
+                                    unsigned long long* pair_counts, int threads) {
+    if (threads < 32 || threads > PAIR_THREADS || threads % 32) return cudaErrorInvalidValue;
     // chunks over all scatterers (for the residue list: over n, the kernel
     // returns early past the list length, which is a handful)
     int64_t chunks = (n + PAIR_CHUNK - 1) / PAIR_CHUNK;
     if (index_list) chunks = 8;
     if (chunks < 1) chunks = 1;
     dim3 grid((unsigned)chunks, (unsigned)num_tiles);
-    project_generic_kernel<BEAM, SPLINE, REF><<<grid, PAIR_THREADS, 0, stream>>>(
+    project_generic_kernel<BEAM, SPLINE, REF, DEG><<<grid, threads, 0, stream>>>(
         xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, basis, bins, p, b,
         REF ? nullptr : boxes, pair_counts);
     return cudaGetLastError();
@@ -1316,18 +1320,27 @@ cudaError_t launch_project_generic(const float4* xyza, const float4* cps, const 
                                    const LineGeom* lines, const int* line_ids, const LineTile* tiles, int num_tiles,
                                    const LineBasis* basis, const SimParams& p, const BeamDev& b,
                                    unsigned long long* bins, cudaStream_t stream, const TileBox* boxes,
-                                   unsigned long long* pair_counts) {
+                                   unsigned long long* pair_counts, int threads) {
     (void)num_cs;
     if (n <= 0 || num_tiles <= 0) return cudaSuccess;
     const bool spline = cps != nullptr;
     const bool ref = p.mode == MODE_REFERENCE;
-#define BCSIM_GEN(B, S, R) launch_generic_t<B, S, R>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream, boxes, pair_counts)
+#define BCSIM_GEN(B, S, R, G) launch_generic_t<B, S, R, G>(xyza, cps, amps, n, degree, index_list, counts, list_lo, lines, line_ids, tiles, num_tiles, basis, p, b, bins, stream, boxes, pair_counts, threads)
+    // cubic splines (the reference's and the workloads' degree) get a kernel
+    // with the degree fixed at compile time
+    const bool cubic = spline && degree == 3;
     if (b.type == BEAM_GAUSSIAN) {
-        if (spline) return ref ? BCSIM_GEN(BEAM_GAUSSIAN, true, true) : BCSIM_GEN(BEAM_GAUSSIAN, true, false);
-        return ref ? BCSIM_GEN(BEAM_GAUSSIAN, false, true) : BCSIM_GEN(BEAM_GAUSSIAN, false, false);
+        if (spline) {
+            if (ref) return cubic ? BCSIM_GEN(BEAM_GAUSSIAN, true, true, 3) : BCSIM_GEN(BEAM_GAUSSIAN, true, true, -1);
+            return cubic ? BCSIM_GEN(BEAM_GAUSSIAN, true, false, 3) : BCSIM_GEN(BEAM_GAUSSIAN, true, false, -1);
+        }
+        return ref ? BCSIM_GEN(BEAM_GAUSSIAN, false, true, -1) : BCSIM_GEN(BEAM_GAUSSIAN, false, false, -1);
     }
-    if (spline) return ref ? BCSIM_GEN(BEAM_LUT, true, true) : BCSIM_GEN(BEAM_LUT, true, false);
-    return ref ? BCSIM_GEN(BEAM_LUT, false, true) : BCSIM_GEN(BEAM_LUT, false, false);
+    if (spline) {
+        if (ref) return cubic ? BCSIM_GEN(BEAM_LUT, true, true, 3) : BCSIM_GEN(BEAM_LUT, true, true, -1);
+        return cubic ? BCSIM_GEN(BEAM_LUT, true, false, 3) : BCSIM_GEN(BEAM_LUT, true, false, -1);
+    }
+    return ref ? BCSIM_GEN(BEAM_LUT, false, true, -1) : BCSIM_GEN(BEAM_LUT, false, false, -1);
 #undef BCSIM_GEN
 }
 
