@@ -6,9 +6,14 @@
 // overlap on the GPU, joined back into one origin stream.  From the second run
 // with unchanged configurations on, that whole multi-stream submission is
 // replayed as one captured CUDA graph, so a batch of many small jobs costs one
-// graph launch instead of tens of kernel launches per job.
+// graph launch instead of tens of kernel launches per job.  Jobs go in largest
+// first (scatterers x lines); with host outputs, each job's IQ is copied to the
+// host as soon as that job is done -- an event per job, recorded by the
+// submission (an external event node of the graph) -- while the others still
+// run, smallest jobs' copies first.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -29,6 +34,9 @@ struct bcsim_batch {
     cudaStream_t origin = nullptr;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> joins;
+    std::vector<cudaEvent_t> done;    // job i's device work finished (its IQ can be copied)
+    cudaStream_t copy = nullptr;      // host copies of the IQ, job by job
+    int* flags = nullptr;             // pinned copies of the jobs' device error flags
     cudaGraphExec_t exec = nullptr;
     std::vector<uint64_t> versions;   // configurations the graph was captured for
     std::vector<void*> outs;          // outputs the graph writes
@@ -38,7 +46,10 @@ struct bcsim_batch {
     ~bcsim_batch() {
         if (exec) cudaGraphExecDestroy(exec);
         for (auto e : joins) cudaEventDestroy(e);
+        for (auto e : done) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
+        if (copy) cudaStreamDestroy(copy);
+        if (flags) cudaFreeHost(flags);
         if (origin) cudaStreamDestroy(origin);
     }
 };
@@ -51,13 +62,31 @@ namespace {
         if (e_ != cudaSuccess) throw SimError(BCSIM_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-void enqueue_all(bcsim_batch* b, const std::vector<float2*>& outs) {
+// The jobs' sizes (scatterers x lines), the order of submission and of copies.
+std::vector<double> job_costs(bcsim_batch* b) {
+    std::vector<double> cost(b->handles.size());
+    for (size_t i = 0; i < cost.size(); i++) {
+        const Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+        cost[i] = (double)s.total_num_scatterers() * (double)s.num_lines();
+    }
+    return cost;
+}
+
+void enqueue_all(bcsim_batch* b, const std::vector<float2*>& outs, bool capturing) {
     BATCH_CUDA(cudaEventRecord(b->fork, b->origin));
-    for (size_t i = 0; i < b->handles.size(); i++) {
+    const std::vector<double> cost = job_costs(b);
+    std::vector<size_t> order(cost.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+    for (size_t i : order) {
         Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
         cudaStream_t st = s.stream();
         BATCH_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
         s.enqueue(st, outs[i], false);
+        // seen outside the graph too when captured, so that the host copy of
+        // this job's IQ can wait for it alone
+        if (capturing) BATCH_CUDA(cudaEventRecordWithFlags(b->done[i], st, cudaEventRecordExternal));
+        else BATCH_CUDA(cudaEventRecord(b->done[i], st));
         BATCH_CUDA(cudaEventRecord(b->joins[i], st));
         BATCH_CUDA(cudaStreamWaitEvent(b->origin, b->joins[i], 0));
     }
@@ -88,7 +117,7 @@ void run(bcsim_batch* b, const std::vector<float2*>& outs) {
     bool noisy = false;
     for (size_t i = 0; i < n; i++) noisy = noisy || bcsim_gb300::simulator_of(b->handles[i]).noisy();
     if (!b->use_graph || b->runs_since_change == 0 || noisy) {
-        enqueue_all(b, outs);
+        enqueue_all(b, outs, false);
         b->runs_since_change++;
         return;
     }
@@ -96,7 +125,7 @@ void run(bcsim_batch* b, const std::vector<float2*>& outs) {
         cudaGraph_t graph = nullptr;
         BATCH_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed));
         try {
-            enqueue_all(b, outs);
+            enqueue_all(b, outs, true);
         } catch (...) {
             cudaStreamEndCapture(b->origin, &graph);
             if (graph) cudaGraphDestroy(graph);
@@ -143,8 +172,12 @@ int bcsim_batch_create(bcsim_handle* const* handles, int count, int use_graph, b
         if (count > 0) bcsim_gb300::simulator_of(b->handles[0]).stream();   // device ready
         BATCH_CUDA(cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking));
         BATCH_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        BATCH_CUDA(cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
         b->joins.resize(count);
         for (auto& e : b->joins) BATCH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->done.resize(count);
+        for (auto& e : b->done) BATCH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        if (count > 0) BATCH_CUDA(cudaMallocHost(&b->flags, (size_t)count * sizeof(int)));
     });
     if (rc != BCSIM_OK) {
         delete b;
@@ -174,15 +207,30 @@ int bcsim_batch_run(bcsim_batch* b, float* const* host_outs, const int64_t* caps
         }
         run(b, outs);
         if (host_outs) {
-            for (size_t i = 0; i < n; i++) {
+            // each job's IQ as soon as that job is done, smallest jobs first
+            // (they finish first), while the others still run
+            const std::vector<double> cost = job_costs(b);
+            std::vector<size_t> order(n);
+            for (size_t i = 0; i < n; i++) order[i] = i;
+            std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] < cost[y]; });
+            for (size_t i : order) {
                 if (!host_outs[i]) continue;
                 Simulator& s = bcsim_gb300::simulator_of(b->handles[i]);
+                BATCH_CUDA(cudaStreamWaitEvent(b->copy, b->done[i], 0));
                 BATCH_CUDA(cudaMemcpyAsync(host_outs[i], outs[i], (size_t)s.num_lines() * s.num_out_samples() * sizeof(float2),
-                                           cudaMemcpyDeviceToHost, b->origin));
+                                           cudaMemcpyDeviceToHost, b->copy));
             }
         }
+        // every job's bounded-wait error flag, read in the same synchronisation;
+        // a job whose flag is set reports (and clears) it
+        for (size_t i = 0; i < n; i++) {
+            BATCH_CUDA(cudaStreamWaitEvent(b->copy, b->done[i], 0));
+            BATCH_CUDA(bcsim_gb300::simulator_of(b->handles[i]).enqueue_flag_read(b->flags + i, b->copy));
+        }
+        BATCH_CUDA(cudaStreamSynchronize(b->copy));
         BATCH_CUDA(cudaStreamSynchronize(b->origin));
-        for (size_t i = 0; i < n; i++) bcsim_gb300::simulator_of(b->handles[i]).check_device_flag();
+        for (size_t i = 0; i < n; i++)
+            if (b->flags[i]) bcsim_gb300::simulator_of(b->handles[i]).check_device_flag();
     });
 }
 
