@@ -24,6 +24,13 @@ convolution, demodulation, decimation).  Prints one JSON line on rank 0.
   pairs of weight 0), and its HBM traffic.
 * cpu_baseline: the CPU port of the reference algorithm (oracle, reference float
   arithmetic, FFT convolution) on all host cores, on a subset of the lines.
+* rel_rms: the timed step's IQ against the FP64 CPU oracle on a spread of lines.
+* batch: the 64 uneven jobs of the batch workload as one Batch.run against one
+  simulate_lines per job (IQ to the host in both), and the batched output's
+  IQ error against the FP64 oracle on a sample of jobs and lines.
+* serve: Poisson request streams at 200, 1000 and 3000 requests/s over 8
+  resident phantoms, served by the continuous-batching server and, live, by
+  serial plain execution: latency percentiles and throughput of both.
 
 Lines are independent, so N GPUs run N independent replicas of the workload
 (weak scaling, no collective).
@@ -570,6 +577,21 @@ def batch_section(args):
     t_batch = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
     n_spline = sum(1 for j in jobs if j.splines)
+    # the batched output against the FP64 oracle: the eight smallest jobs whole,
+    # eight lines spread over each of four of the largest (outside the timing)
+    from oracle import oracle as O
+
+    order = sorted(range(len(jobs)), key=lambda k: jobs[k].projections)
+    errs = []
+    t0 = time.perf_counter()
+    for k in order[:8]:
+        errs.append(O.rel_rms(outs[k], O.simulate(jobs[k], O.MODE_FP64)))
+    for k in order[-4:]:
+        L = jobs[k].scan.num_lines
+        idx = np.unique(np.linspace(0, L - 1, 8).round().astype(int))
+        errs.append(O.rel_rms(outs[k][idx], O.simulate(_subset_idx(jobs[k], idx), O.MODE_FP64)))
+    check = {"max": max(errs), "tolerance": 1e-4, "jobs_checked": len(errs), "oracle_s": time.perf_counter() - t0,
+             "sample": "the 8 smallest jobs whole, 8 spread lines of each of the 4 largest"}
     return {"workload": f"batch_uneven: {len(jobs)} jobs ({n_spline} spline), {total:.4e} projections per step, "
                         f"scale {args.batch_scale}",
             "unit": "projections/s", "steps": steps,
@@ -577,7 +599,7 @@ def batch_section(args):
             "plain": {"value": total / t_plain, "ms_per_step": t_plain * 1e3,
                       "form": "one simulate_lines per job, in order, IQ to the host"},
             "batched_over_plain": t_plain / t_batch, "io": "IQ to the host every step (both forms)",
-            "clocks": clk}
+            "rel_rms": check, "clocks": clk}
 
 
 def run_batch(args):
