@@ -13,6 +13,10 @@
   MakeGaussianExcitation<float> (src/utils/GaussPulse.cpp:52-70) returns for
   the pulses of the benchmark workloads and a spread of others
   (`python tests/golden/make_golden.py excitation`).
+* ref_full_<workload>.npz -- the reference's own IQ for 32 lines spread over
+  each full-size benchmark workload (2-D sector, 3-D LUT volume, spline
+  sector; their inputs are regenerated from the workloads' seeds), with the
+  line indices (`python tests/golden/make_golden.py full`).
 * ref_<case>.npz -- inputs of a small seeded case, the IQ that the reference's
   own CPU algorithm returns for them (bcsim::Create("cpu")->simulate_lines), and
   the time-projection bins of a few lines from its projection loops
@@ -193,6 +197,28 @@ def make_excitation():
     print("excitation", os.path.getsize(os.path.join(HERE, "ref_excitation.npz")))
 
 
+FULL_WORKLOADS = ["sector_2d_fixed", "volume_3d_lut", "sector_spline"]
+
+
+def full_lines(L: int) -> np.ndarray:
+    return np.unique(np.linspace(0, L - 1, 32).round().astype(int))
+
+
+def make_full():
+    import copy
+
+    for name in FULL_WORKLOADS:
+        job = getattr(W, name)()
+        idx = full_lines(job.scan.num_lines)
+        sub = copy.copy(job)
+        s = job.scan
+        sub.scan = W.ScanSequence(s.origins[idx], s.directions[idx], s.lateral_dirs[idx], s.timestamps[idx],
+                                  s.line_length)
+        iq = O.ref_simulate(sub, threads=0)
+        np.savez_compressed(os.path.join(HERE, f"ref_full_{name}.npz"), lines=idx, ref_iq=iq)
+        print(name, iq.shape, os.path.getsize(os.path.join(HERE, f"ref_full_{name}.npz")))
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("oracle/_ref/libbcsim_ref.so is missing: run `make -C oracle all` where the reference sources are")
@@ -214,7 +240,10 @@ if __name__ == "__main__":
         make_imaging()
     elif sys.argv[1:] == ["excitation"]:
         make_excitation()
+    elif sys.argv[1:] == ["full"]:
+        make_full()
     else:
         main()
         make_imaging()
         make_excitation()
+        make_full()

@@ -270,6 +270,25 @@ def test_full_size_frames_vs_oracle(oracle, which):
     assert worst <= 10 * FP64_TOL, (which, worst)
 
 
+@pytest.mark.parametrize("which", ["sector_2d_fixed", "volume_3d_lut", "sector_spline"])
+def test_full_size_vs_reference_iq(oracle, which):
+    """The full-size workloads on the GPU against the IQ that the reference's
+    own CPU algorithm returned for 32 spread lines of each
+    (tests/golden/ref_full_*.npz): the reference-arithmetic mode within the
+    reference's float FFT, the fp64 mode within the reference's own FP32
+    error against FP64."""
+    import os
+
+    from conftest import GOLDEN
+    from openbcsim_gb300 import workloads as W
+
+    z = np.load(os.path.join(GOLDEN, f"ref_full_{which}.npz"))
+    job = getattr(W, which)()
+    idx = z["lines"]
+    assert oracle.rel_rms(run(job, "reference")[idx], z["ref_iq"]) <= REF_IQ_TOL
+    assert oracle.rel_rms(run(job)[idx], z["ref_iq"]) <= 3e-3
+
+
 def test_render_once_at_shared_timestamp(oracle):
     """Splines that every line sees at one timestamp from one origin are
     rendered once into shared-origin records (the reference renders them to

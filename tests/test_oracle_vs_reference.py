@@ -62,3 +62,32 @@ def test_oracle_errors_match_reference_messages(oracle):
     # reaching the caller; the oracle and the engine report it as an error
     with pytest.raises(RuntimeError, match="could not determine knot interval"):
         oracle.simulate(job)
+
+
+def _full_subset(name):
+    import copy
+    import os
+
+    from conftest import GOLDEN
+    from openbcsim_gb300 import workloads as W
+
+    z = np.load(os.path.join(GOLDEN, f"ref_full_{name}.npz"))
+    job = getattr(W, name)()
+    idx = z["lines"]
+    sub = copy.copy(job)
+    s = job.scan
+    sub.scan = W.ScanSequence(s.origins[idx], s.directions[idx], s.lateral_dirs[idx], s.timestamps[idx],
+                              s.line_length)
+    return sub, z["ref_iq"]
+
+
+@pytest.mark.parametrize("name", ["sector_2d_fixed", "volume_3d_lut", "sector_spline"])
+def test_full_size_workloads_pinned(oracle, name):
+    """The full-size benchmark workloads (inputs from their seeds): 32 lines
+    spread over each, against the IQ that the reference's own CPU algorithm
+    returned for them (tests/golden/ref_full_*.npz).  The REF32 restatement
+    differs only by the reference's float FFT; the FP64 oracle by the
+    reference's FP32 arithmetic."""
+    sub, ref_iq = _full_subset(name)
+    assert oracle.rel_rms(oracle.simulate(sub, oracle.MODE_REF32), ref_iq) <= 1e-4
+    assert oracle.rel_rms(oracle.simulate(sub, oracle.MODE_FP64), ref_iq) <= REF_VS_FP64_TOL
