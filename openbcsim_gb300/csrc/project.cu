@@ -390,17 +390,19 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
 }
 
 // One CTA: a chunk of `chunk` (<= 1024) consecutive records, sorted by bin,
-// staged once in shared memory by a TMA bulk copy; then, for every group of
-// blockDim lines (one per thread, in direction order so that a warp's 32 lines
-// point in nearby directions), two phases per warp:
+// staged once in shared memory by a TMA bulk copy; then the lines, in slots of
+// 32 (one line per lane, in direction order so that a slot's lines point in
+// nearby directions), are handed to the warps one slot at a time as the warps
+// finish the previous one (walk lengths differ between slots), two phases per
+// slot:
 //   A. mask: each lane tests one record against the warp's "slot box": the
 //      lateral/elevational ranges outside which every line of the slot has
 //      weight exactly 0 (the lookup table's extent, or where exp2 underflows),
 //      widened by the spread of the slot's line frames (along the slot's
 //      radial direction times the record's radial coordinate, normal to it times
-//      the record's distance from the axis).  32 records per instruction; one
-//      ballot word per 32 records, word w kept by lane w.
-//   B. walk: only the records whose bit is set, in bin order.  A line's
+//      the record's distance from the axis).  32 records per instruction; the
+//      selection kept transposed (lane l, bit w: record 32 w + l).
+//   B. walk: only the selected records, in bin order.  A line's
 //      contributions to one bin are summed in FP32, folded into an int64 total
 //      at absolute record indices k*p.fold, and written when the bin changes: a
 //      plain store for bins strictly inside the chunk (no other CTA holds
@@ -415,7 +417,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                           SimParams p, BeamDev b, int lut_planes, unsigned long long* __restrict__ pair_counts) {
     extern __shared__ __align__(128) float4 sm[];
     __shared__ __align__(8) uint64_t bar;
-    __shared__ int s_lut_base, s_lut_planes;
+    __shared__ int s_lut_base, s_lut_planes, s_next_slot;
     // segments of the chunk: record index ranges [s_seg[k], s_seg[k+1]) within
     // one bin and one fold group (the walk folds and stores only at their ends)
     __shared__ int s_seg[1024 + 2];
@@ -447,6 +449,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         }
         s_lut_base = base;
         s_lut_planes = planes;
+        s_next_slot = blockDim.x >> 5;
     }
     __syncthreads();
     const int lut_base = s_lut_base, lut_staged = s_lut_planes;
@@ -553,19 +556,22 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         __syncthreads();
     }
 
-    for (int g0 = 0; g0 < L; g0 += blockDim.x) {
-        if (g0 + (tid & ~31) >= L) break;   // this warp has no line in this group (nor in later ones)
-        const int slot_pos = g0 + tid;
+    // slots of 32 lines are handed out to the warps as they finish the previous
+    // one, so that warps with short walks take more slots
+    const int nslots = (L + 31) >> 5;
+    for (int slot = tid >> 5; slot < nslots;) {
+        const int slot_pos = (slot << 5) + lane;
         const bool active = slot_pos < L;
         const int line = __ldg(line_order + (active ? slot_pos : L - 1));
         const LineK q = load_line<BEAM, REF>(lines + line, b);
         unsigned long long* lb = bins + (int64_t)line * p.ns * stride;
 
         // ---- phase A: records this warp's lines can see ----
-        unsigned mask = 0xffffffffu;
+        // sel, transposed: bit w of lane l's word <=> record 32 w + l selected
+        unsigned sel;
         bool front_certain = false;
         if (cull) {
-            const SlotCone* c = cones + min(g0 + (tid & ~31), L - 1) / 32;   // warp-uniform
+            const SlotCone* c = cones + slot;   // warp-uniform
             const float lx = __ldg(&c->lx), ly = __ldg(&c->ly), lz = __ldg(&c->lz);
             const float ex = __ldg(&c->ex), ey = __ldg(&c->ey), ez = __ldg(&c->ez);
             const float rx = __ldg(&c->rx), ry = __ldg(&c->ry), rz = __ldg(&c->rz);
@@ -576,7 +582,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             const float cl_c = 0.5f * (p.cull_l_lo + p.cull_l_hi), ce_c = 0.5f * (p.cull_e_lo + p.cull_e_hi);
             const float cl_h = 0.5f * (p.cull_l_hi - p.cull_l_lo) + 1e-6f * (fabsf(p.cull_l_lo) + fabsf(p.cull_l_hi));
             const float ce_h = 0.5f * (p.cull_e_hi - p.cull_e_lo) + 1e-6f * (fabsf(p.cull_e_lo) + fabsf(p.cull_e_hi));
-            mask = 0;
+            sel = 0;
             bool certain = true;   // every selected record in front of every line of the slot
             for (int w = 0; w < nwords; w++) {
                 const int r = (w << 5) + lane;
@@ -604,28 +610,29 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                     // margin of 1e-5 |A| for the rounding of the per-pair dot product
                     sure = !pass || (dt > 0.0f && dt * dt > a2 * ddm2);
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, pass);
-                certain = certain && __all_sync(0xffffffffu, sure);
-                if (lane == w) mask = m;
+                sel |= (unsigned)pass << w;
+                certain = certain && sure;
             }
-            front_certain = certain;
+            front_certain = __all_sync(0xffffffffu, certain);
+        } else {
+            // every record of the chunk: words 0 .. cnt/32 - 1 full, then cnt % 32 lanes
+            const int full = cnt >> 5;
+            sel = (full >= 32 ? 0xffffffffu : (1u << full) - 1u) | (lane < (cnt & 31) ? 1u << full : 0u);
         }
 
         // ---- phase B: walk the selected records in order ----
-        // Only words with selected records are visited (lane w holds word w).  A
-        // record past the current segment's end closes it: its FP32 run is folded
-        // into the integer total, and at a bin change the total is stored (a
-        // plain store inside the chunk, an atomic at its edge bins: other CTAs
-        // hold records there).  Segments without a selected record cost nothing.
+        // Segment by segment (one FP32 run each), the words of the segment with a
+        // selected record, their bits in order; all of this control is warp-uniform
+        // (segment bounds through redux, words through ballot).  A segment's run is
+        // folded into the integer total at its end, and at a bin change the total
+        // is stored (a plain store inside the chunk, an atomic at its edge bins:
+        // other CTAs hold records there).  Segments without a selected record cost
+        // a few instructions and no fold.
         // COUNT: pairs visited, pairs with a non-zero weight, walk steps in which
         // no lane of the warp had a non-zero weight
         unsigned walked = 0, weighted = 0, idle_steps = 0;
-        const unsigned mask_w = cull ? mask
-                                     : (lane < nwords ? ((lane == nwords - 1 && (cnt & 31)) ? (1u << (cnt & 31)) - 1u
-                                                                                            : 0xffffffffu)
-                                                      : 0u);
-        unsigned nz = __ballot_sync(0xffffffffu, mask_w != 0u);
-        int cur = first_bin, sg = 0, seg_end = s_seg[1];
+        const unsigned nzw = __reduce_or_sync(0xffffffffu, sel);   // bit w: word w has a selected record
+        int cur = first_bin;
         long long tr = 0, ti = 0;
         float ar = 0.0f, ai = 0.0f;
         auto store_bin = [&]() {
@@ -643,30 +650,33 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         auto walk = [&](auto nodot_tag, auto staged_tag) {
             constexpr bool NODOT = decltype(nodot_tag)::value;
             constexpr bool STAGED = decltype(staged_tag)::value;
-            while (nz) {
-                const int w = __ffs(nz) - 1;
-                nz &= nz - 1u;
-                unsigned word = __shfl_sync(0xffffffffu, mask_w, w);
-                while (word) {
+            for (int sg = 0;; sg++) {
+                const int s0 = __reduce_max_sync(0xffffffffu, s_seg[sg]);
+                if (s0 >= cnt) break;
+                const int s1 = __reduce_max_sync(0xffffffffu, s_seg[sg + 1]);
+                const int w0 = s0 >> 5, w1 = (s1 - 1) >> 5;
+                unsigned wm = nzw & (0xffffffffu << w0) & (0xffffffffu >> (31 - w1));
+                if (!wm) continue;
+                const int nb = __reduce_max_sync(0xffffffffu, __float_as_int(smB[s0].w));
+                if (nb != cur) {
+                    store_bin();
+                    tr = 0;
+                    ti = 0;
+                    cur = nb;
+                }
+                ar = 0.0f;
+                ai = 0.0f;
+                do {
+                    const int w = __ffs(wm) - 1;
+                    wm &= wm - 1u;
+                    unsigned word = __ballot_sync(0xffffffffu, (sel >> w) & 1u);
+                    if (w == w0) word &= 0xffffffffu << (s0 & 31);
+                    if (w == w1) word &= 0xffffffffu >> (31 - ((s1 - 1) & 31));
+                    while (word) {
                     const int i = (w << 5) + __ffs(word) - 1;
                     word &= word - 1u;
                     const float4 B = smB[i];
                     const float4 A = smA[i];
-                    if (i >= seg_end) {   // warp-uniform
-                        tr += f2ll_rn(ar * scale);
-                        if (PD) ti += f2ll_rn(ai * scale);
-                        ar = 0.0f;
-                        ai = 0.0f;
-                        do { sg++; } while (s_seg[sg + 1] <= i);
-                        seg_end = s_seg[sg + 1];
-                        const int nb = __float_as_int(B.w);
-                        if (nb != cur) {
-                            store_bin();
-                            tr = 0;
-                            ti = 0;
-                            cur = nb;
-                        }
-                    }
                     float w8;
                     if (REF) {
                         // vector3::dot, x*rx + y*ry + z*rz left to right (vector3.hpp:87-89)
@@ -750,7 +760,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                         weighted += (active && w8 != 0.0f) ? 1u : 0u;
                         idle_steps += __ballot_sync(0xffffffffu, active && w8 != 0.0f) == 0u ? 1u : 0u;
                     }
-                }
+                    }
+                } while (wm);
+                tr += f2ll_rn(ar * scale);
+                if (PD) ti += f2ll_rn(ai * scale);
             }
         };
         using T_ = std::true_type;
@@ -762,8 +775,6 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             if (BEAM == BEAM_LUT && !REF && all_staged) walk(F_{}, T_{});
             else walk(F_{}, F_{});
         }
-        tr += f2ll_rn(ar * scale);
-        if (PD) ti += f2ll_rn(ai * scale);
         store_bin();
         if (COUNT) {
             walked = __reduce_add_sync(0xffffffffu, walked);
@@ -774,6 +785,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 atomicAdd(pair_counts + 2, (unsigned long long)idle_steps);
             }
         }
+        int next = 0;
+        if (lane == 0) next = atomicAdd(&s_next_slot, 1);
+        slot = __shfl_sync(0xffffffffu, next, 0);
     }
 }
 
@@ -1238,23 +1252,16 @@ static cudaError_t launch_shared_t(const float4* records, int64_t plane, const i
         // share one record chunk and the lookup-table planes it touches, staged
         // in shared memory (up to two planes: a chunk of <= 1024 records spans
         // far less than a table cell radially in any dense phantom; records
-        // beyond them read the table through the cache).  1024 or 512 threads,
-        // whichever leaves fewer idle lanes in the last group of lines.
+        // beyond them read the table through the cache).  1024 threads: the
+        // warps take the slots of 32 lines one after another as they finish
+        // (measured: 512-thread CTAs, one or two per SM, and a single staged
+        // plane are all slower on the 3-D table workload).
         int lut_planes = 0;
         if (BEAM == BEAM_LUT && !REF && p.lut_smem) {
             const size_t plane_bytes = (size_t)b.nl * (b.ne | 1) * sizeof(float4);
             const size_t budget = 200 * 1024;
             if (smem + plane_bytes <= budget) lut_planes = (budget - smem) / plane_bytes >= 2 ? 2 : 1;
             smem += (size_t)lut_planes * plane_bytes;
-        }
-        const int64_t groups1024 = (L + 1023) / 1024, groups512 = (L + 511) / 512;
-        if (groups512 * 512 < groups1024 * 1024) {
-            auto k = project_shared_kernel<PD, BEAM, REF, 512, COUNT>;
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            k<<<(unsigned)chunks, 512, smem, stream>>>(records, plane, counts, chunk, lines, line_order, cones, L, bins,
-                                                       p, b, lut_planes, pair_counts);
-            return cudaGetLastError();
         }
         auto k = project_shared_kernel<PD, BEAM, REF, 1024, COUNT>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
