@@ -1145,9 +1145,12 @@ void Simulator::prepare() {
         spl_basis_f_.reserve(bf.size() * sizeof(float), stream_);
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_d_.get(), bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_f_.get(), bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+        // sort key: the bin (ns + 2 values) above a 10-bit angular cell (32 x 32
+        // octahedral cells), fewer cell bits where the bins need more than 22
         int end_bit = 1;
         while ((1ll << end_bit) < (int64_t)ns + 2) end_bit++;
-        P.end_bit = end_bit;
+        P.p.cell_bits = std::max(0, std::min(10, 32 - end_bit)) & ~1;
+        P.end_bit = end_bit + P.p.cell_bits;
         reserve_records(rec(), P);
         // records per CTA: enough CTAs to fill the GPU several times over, a
         // multiple of the fold group (512 records when chunks of 512 fill the
@@ -1215,7 +1218,7 @@ void Simulator::enqueue_records(cudaStream_t st, int* launches) {
     BCSIM_CUDA(radix_sort_pairs(R.sort_tmp.get(), &tmp_bytes, R.keys_in.as<uint32_t>(), R.keys_out.as<uint32_t>(),
                                 R.vals_in.as<uint32_t>(), R.vals_out.as<uint32_t>(), N, P.end_bit, st));
     *launches += 3;   // init, count, finish
-    BCSIM_CUDA(launch_count_keys(R.keys_out.as<uint32_t>(), N, ns, R.counts.as<int>(), st));
+    BCSIM_CUDA(launch_count_keys(R.keys_out.as<uint32_t>(), N, ns, P.p.cell_bits, R.counts.as<int>(), st));
     ++*launches;
     BCSIM_CUDA(launch_gather_records(R.vals_out.as<uint32_t>(), R.counts.as<int>(), N, R.recA.as<float4>(),
                                      R.recB.as<float4>(), R.records.as<float4>(), N, st));

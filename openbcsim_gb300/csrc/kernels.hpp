@@ -56,9 +56,10 @@ struct SimParams {
     int cull;
     float cull_l_lo, cull_l_hi, cull_e_lo, cull_e_hi;
     float cull_rho_per_bin;    // upper bound of 1 / (2 fs / c)
-    int wide_cta;              // shared-origin kernel: 1024/512-thread CTAs for >= 512 lines
+    int wide_cta;              // shared-origin kernel: 1024-thread CTAs for >= 512 lines
     int lut_smem;              // wide shared-origin kernel: lookup-table planes in shared memory
     int fold;                  // shared-origin kernel: FP32 run sums folded at record indices k*fold (power of 2)
+    int cell_bits;             // shared-origin records: sort key = bin << cell_bits | angular cell of the direction
     int* err_flag;             // the simulator's device error flag: set to 1 when a bounded wait gives up (may be null)
 };
 
@@ -118,7 +119,8 @@ struct LineBasis {
 // Per scatterer, from a shared line origin: exact bin index (fp64 or reference
 // arithmetic), phase-rotated amplitude and LUT radial coordinate.  Writes sort
 // keys (bin index, or ns for near-origin scatterers that need the per-pair path,
-// or ns+1 for scatterers that no line can see), identity values and the
+// or ns+1 for scatterers that no line can see, shifted left by p.cell_bits above
+// the angular cell of the scatterer's direction), identity values and the
 // unsorted records.
 cudaError_t launch_prep_shared(const float4* xyza, int64_t n, int64_t out_offset, const float origin[3],
                                const SimParams& p, const BeamDev& b, uint32_t* keys, uint32_t* vals,
@@ -131,9 +133,10 @@ cudaError_t launch_prep_shared_spline(const float4* cps, const float* amps, int6
                                       const BeamDev& b, uint32_t* keys, uint32_t* vals, float4* recA,
                                       float4* recB, cudaStream_t stream);
 
-// Sorted keys -> counts: counts[0] = #keys < ns, counts[1] = #keys == ns
-// (counts needs 4 ints).
-cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int* counts, cudaStream_t stream);
+// Sorted keys -> counts: counts[0] = #bins < ns, counts[1] = #bins == ns, with
+// bin = key >> cell_bits (counts needs 4 ints).
+cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int cell_bits, int* counts,
+                              cudaStream_t stream);
 
 // Sorted values -> record planes in bin order (plane B starts at out + plane).
 cudaError_t launch_gather_records(const uint32_t* sorted_vals, const int* counts, int64_t n, const float4* recA,

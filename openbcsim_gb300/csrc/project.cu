@@ -249,6 +249,37 @@ __device__ __forceinline__ PrepOut prep_ref(float fdx, float fdy, float fdz, flo
     return o;
 }
 
+// Angular cell of the direction (x, y, z) from the origin: the octahedral map
+// of the unit sphere onto [-1, 1]^2, 2^(bits/2) cells per axis, numbered in
+// Morton order.  Records of one bin sorted by it form compact patches of
+// directions, so that 32 consecutive records share a small bounding sphere.
+__device__ __forceinline__ uint32_t dir_cell(float x, float y, float z, int bits) {
+    const int h = bits >> 1;
+    const float s = fabsf(x) + fabsf(y) + fabsf(z);
+    if (h <= 0 || !(s > 0.0f)) return 0u;
+    float px = x / s, py = y / s;
+    if (z < 0.0f) {   // the lower hemisphere folded onto the corners
+        const float qx = copysignf(1.0f - fabsf(py), px);
+        const float qy = copysignf(1.0f - fabsf(px), py);
+        px = qx;
+        py = qy;
+    }
+    const int m = (1 << h) - 1;
+    const float half_n = 0.5f * (float)(1 << h);
+    const uint32_t ix = (uint32_t)min(max((int)((px + 1.0f) * half_n), 0), m);
+    const uint32_t iy = (uint32_t)min(max((int)((py + 1.0f) * half_n), 0), m);
+    uint32_t c = 0;
+    for (int k = 0; k < h; k++) c |= (((ix >> k) & 1u) << (2 * k)) | (((iy >> k) & 1u) << (2 * k + 1));
+    return c;
+}
+
+// The sort key of a record: its bin (or ns / ns + 1 for the near-origin and the
+// out-of-range ones) above its angular cell.
+__device__ __forceinline__ uint32_t record_key(const PrepOut& o, const SimParams& p) {
+    const uint32_t cell = o.key < (uint32_t)p.ns ? dir_cell(o.A.x, o.A.y, o.A.z, p.cell_bits) : 0u;
+    return (o.key << p.cell_bits) | cell;
+}
+
 __global__ void prep_shared_kernel(const float4* __restrict__ xyza, int64_t n, int64_t off, double ox, double oy,
                                    double oz, float ofx, float ofy, float ofz, SimParams p, BeamDev b,
                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
@@ -265,7 +296,7 @@ __global__ void prep_shared_kernel(const float4* __restrict__ xyza, int64_t n, i
     } else {
         o = prep_ref(__fsub_rn(q.x, ofx), __fsub_rn(q.y, ofy), __fsub_rn(q.z, ofz), q.w, p, b, false);
     }
-    keys[off + i] = o.key;
+    keys[off + i] = record_key(o, p);
     vals[off + i] = (uint32_t)(off + i);
     recA[off + i] = o.A;
     recB[off + i] = o.B;
@@ -308,14 +339,14 @@ __global__ void prep_shared_spline_kernel(const float4* __restrict__ cps, const 
     } else {
         o = prep_ref(__fsub_rn(fx, ofx), __fsub_rn(fy, ofy), __fsub_rn(fz, ofz), __ldg(amps + i), p, b, true);
     }
-    keys[off + i] = o.key;
+    keys[off + i] = record_key(o, p);
     vals[off + i] = (uint32_t)(off + i);
     recA[off + i] = o.A;
     recB[off + i] = o.B;
 }
 
-// Boundaries of the sorted keys: counts[2] = first index with key >= ns,
-// counts[3] = first index with key > ns (both n if absent).
+// Boundaries of the sorted keys (bin = key >> cell_bits): counts[2] = first
+// index with bin >= ns, counts[3] = first index with bin > ns (both n if absent).
 __global__ void init_counts_kernel(int* counts, int64_t n) {
     counts[0] = 0;
     counts[1] = 0;
@@ -323,12 +354,12 @@ __global__ void init_counts_kernel(int* counts, int64_t n) {
     counts[3] = (int)n;
 }
 
-__global__ void count_keys_kernel(const uint32_t* __restrict__ keys, int64_t n, int ns, int* counts) {
+__global__ void count_keys_kernel(const uint32_t* __restrict__ keys, int64_t n, int ns, int cell_bits, int* counts) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = keys[i];
+    const uint32_t k = keys[i] >> cell_bits;
     const bool first = i == 0;
-    const uint32_t prev = first ? 0u : keys[i - 1];
+    const uint32_t prev = first ? 0u : keys[i - 1] >> cell_bits;
     if (k >= (uint32_t)ns && (first || prev < (uint32_t)ns)) counts[2] = (int)i;
     if (k > (uint32_t)ns && (first || prev <= (uint32_t)ns)) counts[3] = (int)i;
 }
@@ -531,6 +562,32 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     const float ce = 0.5f * (float)(b.ne - 2), he = 0.5f * (float)b.ne;
     const bool cull = !REF && p.cull;
     const int nwords = (cnt + 31) >> 5;
+    // bounding sphere (centre, radius) of each word of 32 records, for the
+    // slots' word test; records of one bin are sorted by the angular cell of
+    // their direction, so a word covers a compact patch of directions
+    __shared__ float4 s_sph[32];
+    if (cull) {
+        const int nwarps = blockDim.x >> 5, wid = tid >> 5;
+        for (int w = wid; w < nwords; w += nwarps) {
+            // the last word's missing lanes repeat the chunk's last record
+            const float4 A = smA[min((w << 5) + lane, cnt - 1)];
+            float x0 = A.x, x1 = A.x, y0 = A.y, y1 = A.y, z0 = A.z, z1 = A.z;
+            for (int o = 16; o > 0; o >>= 1) {
+                x0 = fminf(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+                x1 = fmaxf(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+                y0 = fminf(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+                y1 = fmaxf(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+                z0 = fminf(z0, __shfl_xor_sync(0xffffffffu, z0, o));
+                z1 = fmaxf(z1, __shfl_xor_sync(0xffffffffu, z1, o));
+            }
+            const float cx = 0.5f * (x0 + x1), cy = 0.5f * (y0 + y1), cz = 0.5f * (z0 + z1);
+            const float dx = A.x - cx, dy = A.y - cy, dz = A.z - cz;
+            float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
+            // radius widened past the rounding of the differences and the square root
+            if (lane == 0) s_sph[w] = make_float4(cx, cy, cz, fmaf(sqrtf(d2), 1.0001f, 1e-9f));
+        }
+    }
     {
         // a record starts a segment where its bin differs from its predecessor's
         // or at a fold-group start; ordered compaction: a ballot per warp, then a
@@ -582,9 +639,33 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             const float cl_c = 0.5f * (p.cull_l_lo + p.cull_l_hi), ce_c = 0.5f * (p.cull_e_lo + p.cull_e_hi);
             const float cl_h = 0.5f * (p.cull_l_hi - p.cull_l_lo) + 1e-6f * (fabsf(p.cull_l_lo) + fabsf(p.cull_l_hi));
             const float ce_h = 0.5f * (p.cull_e_hi - p.cull_e_lo) + 1e-6f * (fabsf(p.cull_e_lo) + fabsf(p.cull_e_hi));
+            // word test, lane w for word w: a record A of the word lies within R
+            // of its centre C, so |A.l - C.l| <= R, |A.r| <= |C.r| + R, the part of A
+            // normal to r is at most |C_perp| + R and |A| <= |C| + R.  A word
+            // that fails with these bounds (and tol, past their float rounding)
+            // holds no record that passes the record test below in exact
+            // arithmetic: no line of the slot gives any of its records a weight.
+            bool word_pass = false;
+            if (lane < nwords) {
+                const float4 S = s_sph[lane];
+                const float uC = fmaf(S.z, lz, fmaf(S.y, ly, S.x * lx));
+                const float vC = fmaf(S.z, ez, fmaf(S.y, ey, S.x * ex));
+                const float dtC = fmaf(S.z, rz, fmaf(S.y, ry, S.x * rx));
+                const float c2 = fmaf(S.z, S.z, fmaf(S.y, S.y, S.x * S.x));
+                const float cn = sqrtf(c2);
+                const float apC = sqrtf(fmaf(c2, 4e-6f, fmaxf(fmaf(-dtC, dtC, c2), 0.0f))) * 1.00001f;
+                const float adt = fabsf(dtC) + S.w, apm = apC + S.w;
+                const float su = fmaf(adt, du_par, fmaf(apm, du_perp, S.w));
+                const float sv = fmaf(adt, dv_par, fmaf(apm, dv_perp, S.w));
+                const float tol = 1e-5f * (cn + S.w + su + sv + fabsf(cl_c) + cl_h + fabsf(ce_c) + ce_h);
+                const bool front = fmaf(cn + S.w, sqrtf(dd2), dtC + S.w + tol) >= 0.0f;
+                word_pass = fabsf(uC - cl_c) < cl_h + su + tol && fabsf(vC - ce_c) < ce_h + sv + tol && front;
+            }
+            const unsigned words = __ballot_sync(0xffffffffu, word_pass);
             sel = 0;
             bool certain = true;   // every selected record in front of every line of the slot
             for (int w = 0; w < nwords; w++) {
+                if (!((words >> w) & 1u)) continue;   // warp-uniform
                 const int r = (w << 5) + lane;
                 bool pass = false, sure = true;
                 if (r < cnt) {
@@ -1220,11 +1301,13 @@ cudaError_t launch_prep_shared_spline(const float4* cps, const float* amps, int6
     return cudaGetLastError();
 }
 
-cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int* counts, cudaStream_t stream) {
+cudaError_t launch_count_keys(const uint32_t* sorted_keys, int64_t n, int ns, int cell_bits, int* counts,
+                              cudaStream_t stream) {
     init_counts_kernel<<<1, 1, 0, stream>>>(counts, n);
     if (n > 0) {
         const int threads = 256;
-        count_keys_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(sorted_keys, n, ns, counts);
+        count_keys_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(sorted_keys, n, ns,
+                                                                                        cell_bits, counts);
     }
     finish_counts_kernel<<<1, 1, 0, stream>>>(counts);
     return cudaGetLastError();
