@@ -1146,10 +1146,14 @@ void Simulator::prepare() {
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_d_.get(), bd.data(), bd.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         BCSIM_CUDA(cudaMemcpyAsync(spl_basis_f_.get(), bf.data(), bf.size() * sizeof(float), cudaMemcpyHostToDevice, st));
         // sort key: the bin (ns + 2 values) above a 10-bit angular cell (32 x 32
-        // octahedral cells), fewer cell bits where the bins need more than 22
+        // octahedral cells), fewer cell bits where the bins need more than 22.
+        // Cells only where a bin holds two words of records on average: with
+        // fewer, a word spans several bins and the cells buy nothing for their
+        // radix-sort pass and the kernel's word test.  (Not tied to culling, so
+        // that culling on and off see the same record order.)
         int end_bit = 1;
         while ((1ll << end_bit) < (int64_t)ns + 2) end_bit++;
-        P.p.cell_bits = std::max(0, std::min(10, 32 - end_bit)) & ~1;
+        P.p.cell_bits = N >= 64 * (int64_t)ns ? std::max(0, std::min(10, 32 - end_bit)) & ~1 : 0;
         P.end_bit = end_bit + P.p.cell_bits;
         reserve_records(rec(), P);
         // records per CTA: enough CTAs to fill the GPU several times over, a

@@ -452,6 +452,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     // segments of the chunk: record index ranges [s_seg[k], s_seg[k+1]) within
     // one bin and one fold group (the walk folds and stores only at their ends)
     __shared__ int s_seg[1024 + 2];
+    __shared__ unsigned short s_seg_of[1024];   // segment of each record
     __shared__ int s_seg_warp[32];
     const int n_valid = __ldg(counts);
     const int64_t start = (int64_t)blockIdx.x * chunk;
@@ -566,7 +567,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
     // slots' word test; records of one bin are sorted by the angular cell of
     // their direction, so a word covers a compact patch of directions
     __shared__ float4 s_sph[32];
-    if (cull) {
+    const bool word_test = cull && p.cell_bits > 0;
+    if (word_test) {
         const int nwarps = blockDim.x >> 5, wid = tid >> 5;
         for (int w = wid; w < nwords; w += nwarps) {
             // the last word's missing lanes repeat the chunk's last record
@@ -604,6 +606,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             int off = total;
             for (int k = 0; k < wid; k++) off += s_seg_warp[k];
             if (start) s_seg[off + __popc(bal & ((1u << lane) - 1u))] = r;
+            if (r < cnt) s_seg_of[r] = (unsigned short)(off + __popc(bal & ((2u << lane) - 1u)) - 1);
             for (int k = 0; k < nwarps; k++) total += s_seg_warp[k];
             __syncthreads();
         }
@@ -645,8 +648,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
             // that fails with these bounds (and tol, past their float rounding)
             // holds no record that passes the record test below in exact
             // arithmetic: no line of the slot gives any of its records a weight.
-            bool word_pass = false;
-            if (lane < nwords) {
+            bool word_pass = lane < nwords;
+            if (word_test && word_pass) {
                 const float4 S = s_sph[lane];
                 const float uC = fmaf(S.z, lz, fmaf(S.y, ly, S.x * lx));
                 const float vC = fmaf(S.z, ez, fmaf(S.y, ey, S.x * ex));
@@ -728,16 +731,28 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 }
             }
         };
+        // the first selected record at or after record s (cnt if none)
+        auto next_selected = [&](int s) -> int {
+            if (s >= cnt) return cnt;
+            const int w = s >> 5;
+            const unsigned word = __ballot_sync(0xffffffffu, (sel >> w) & 1u) & (0xffffffffu << (s & 31));
+            if (word) return (w << 5) + __ffs(word) - 1;
+            const unsigned rest = w >= 31 ? 0u : nzw & (0xfffffffeu << w);
+            if (!rest) return cnt;
+            const int w2 = __ffs(rest) - 1;
+            return (w2 << 5) + __ffs(__ballot_sync(0xffffffffu, (sel >> w2) & 1u)) - 1;
+        };
         auto walk = [&](auto nodot_tag, auto staged_tag) {
             constexpr bool NODOT = decltype(nodot_tag)::value;
             constexpr bool STAGED = decltype(staged_tag)::value;
-            for (int sg = 0;; sg++) {
-                const int s0 = __reduce_max_sync(0xffffffffu, s_seg[sg]);
-                if (s0 >= cnt) break;
+            // from the first selected record on, segment by segment: the segment
+            // of the next selected record, its selected records from there to
+            // its end, then the next selected record past it
+            for (int s0 = next_selected(0); s0 < cnt;) {
+                const int sg = __reduce_max_sync(0xffffffffu, (int)s_seg_of[s0]);
                 const int s1 = __reduce_max_sync(0xffffffffu, s_seg[sg + 1]);
                 const int w0 = s0 >> 5, w1 = (s1 - 1) >> 5;
                 unsigned wm = nzw & (0xffffffffu << w0) & (0xffffffffu >> (31 - w1));
-                if (!wm) continue;
                 const int nb = __reduce_max_sync(0xffffffffu, __float_as_int(smB[s0].w));
                 if (nb != cur) {
                     store_bin();
@@ -845,6 +860,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
                 } while (wm);
                 tr += f2ll_rn(ar * scale);
                 if (PD) ti += f2ll_rn(ai * scale);
+                s0 = next_selected(s1);
             }
         };
         using T_ = std::true_type;
