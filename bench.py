@@ -53,7 +53,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "scatterer-line projections/s"
 # DRAM traffic of one projection launch of the default workloads (ncu, full size)
-NCU_TRAFFIC_BYTES = {"volume_3d_lut": 395.99e6 + 354.79e6}
+NCU_TRAFFIC_BYTES = {"volume_3d_lut": 380.37e6 + 359.62e6}
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -629,10 +629,19 @@ def serve_stream(args, phantoms, sims, rate, seconds):
     reqs = W.request_stream(phantoms, rate_hz=rate, seconds=seconds)
     server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4, max_in_flight=args.max_in_flight)
     pids = [server.add_phantom(s) for s in sims]
-    for k, s in enumerate(phantoms):   # warm-up: one request per phantom
+    # warm-up: per phantom, as many requests of the stream's largest shape (256
+    # lines, decimation 4) as can be in flight at once, so that the slots the
+    # stream uses have grown before it starts
+    big = W.sector_scan(256, 35.0, 0.12)
+    for k, s in enumerate(phantoms):
         sc = s.scan
         server.wait(server.submit(pids[k], sc.origins, sc.directions, sc.line_length, sc.lateral_dirs,
                                   sc.timestamps, 8))
+        warm = [server.submit(pids[k], big.origins, big.directions, big.line_length, big.lateral_dirs,
+                              np.full(256, float(sc.timestamps[0]), np.float32), 4)
+                for _ in range(args.max_in_flight)]
+        for rid in warm:
+            server.wait(rid)
     # the client: this thread submits at the arrival times, a second one
     # collects the results in order as they complete
     ids = queue.Queue()
