@@ -365,6 +365,28 @@ def test_culling_is_exact_full_volume():
     assert np.array_equal(run(job, cull="on"), run(job, cull="off"))
 
 
+@pytest.mark.parametrize("beam", ["lut", "gaussian"])
+def test_word_test_is_exact(oracle, beam):
+    """Dense phantoms (at least 64 records per bin): the records of a bin are
+    ordered by the angular cell of their direction, and each slot first tests
+    whole 32-record words by their bounding spheres.  A word the test skips
+    holds no pair of non-zero weight: culling on and off are bit-identical,
+    and the IQ matches the FP64 oracle."""
+    from openbcsim_gb300 import workloads as W
+
+    if beam == "lut":
+        job = W.volume_3d_lut(num_scatterers=700_000, n_az=40, n_el=24)
+    else:
+        job = W.sector_2d_fixed(num_scatterers=600_000, num_lines=128)
+    assert job.num_scatterers >= 64 * job.num_samples   # the angular order and the word test are on
+    on = run(job, cull="on")
+    assert np.array_equal(on, run(job, cull="off"))
+    L = job.scan.num_lines
+    for lo in (0, L // 2, L - 3):
+        ref = oracle.simulate(job, oracle.MODE_FP64, line_begin=lo, line_end=lo + 3)
+        assert oracle.rel_rms(on[lo:lo + 3], ref) <= FP64_TOL
+
+
 @pytest.mark.parametrize("num_scatterers,lut_shape", [(300_000, (256, 64, 64)),   # dense: chunks within 1-2 planes
                                                       (20_000, (256, 64, 64)),    # sparse: chunks span many planes
                                                       (100_000, (64, 96, 80))])   # one staged plane fits
