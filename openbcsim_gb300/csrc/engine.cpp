@@ -90,6 +90,16 @@ Simulator::Simulator() = default;
 
 Simulator::~Simulator() {   // buffers freed in stream order, then the streams (OwnedStream)
     for (cudaEvent_t e : ev_blocks_) cudaEventDestroy(e);
+    drop_timings();
+}
+
+// Stage intervals of a timed call that did not finish (an error on the way).
+void Simulator::drop_timings() {
+    for (PendingTiming& t : pending_timings_) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    pending_timings_.clear();
 }
 
 void Simulator::log(int level, const std::string& msg) const {
@@ -828,32 +838,51 @@ static std::vector<float4> pack_lut(const std::vector<float>& c, int nr, int nl,
 // simulate
 // ---------------------------------------------------------------------------
 namespace {
+// Stage timer of store_kernel_details: stop() records the interval's end and
+// hands both events to the simulator's pending list without waiting, so that
+// timing a simulation does not hold the host between its stages (a wait there
+// would leave the GPU idle until the next stage is launched); the intervals are
+// read once the simulation has finished (Simulator::resolve_timings).
 struct EventTimer {
     bool on;
     cudaStream_t s;
-    cudaEvent_t a = nullptr, b = nullptr;
-    EventTimer(bool enabled, cudaStream_t st) : on(enabled), s(st) {
+    std::vector<PendingTiming>* out;
+    cudaEvent_t a = nullptr;
+    EventTimer(bool enabled, cudaStream_t st, std::vector<PendingTiming>* pending)
+        : on(enabled), s(st), out(pending) {
         if (on) {
             cudaEventCreate(&a);
-            cudaEventCreate(&b);
             cudaEventRecord(a, s);
         }
     }
     ~EventTimer() {
         if (a) cudaEventDestroy(a);
-        if (b) cudaEventDestroy(b);
     }
     void restart() { if (on) cudaEventRecord(a, s); }
-    double stop() {
-        if (!on) return 0.0;
+    void stop(const char* key) {
+        if (!on) return;
+        cudaEvent_t b = nullptr;
+        cudaEventCreate(&b);
         cudaEventRecord(b, s);
-        cudaEventSynchronize(b);
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, a, b);
-        return ms;
+        out->push_back({key, a, b});
+        // a fresh start event: the handed-over one keeps its timestamp
+        cudaEventCreate(&a);
+        cudaEventRecord(a, s);
     }
 };
 }  // namespace
+
+// The pending stage intervals, in the order they were stopped, into debug_.
+void Simulator::resolve_timings() {
+    for (PendingTiming& t : pending_timings_) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(t.b) == cudaSuccess && cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess)
+            debug_[t.key].push_back(ms);
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    pending_timings_.clear();
+}
 
 // ---------------------------------------------------------------------------
 // prepare: everything the host computes or uploads for one configuration
@@ -1239,8 +1268,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     const BeamDev& b = P.b;
     const int L = num_lines_;
     const int ns = (int)ns_;
-    EventTimer total(timing, st);
-    EventTimer timer(timing, st);
+    EventTimer total(timing, st, &pending_timings_);
+    EventTimer timer(timing, st, &pending_timings_);
     unsigned long long* bins = bins_[cur_].as<unsigned long long>();
     RecordSet& R = rec();
     int launches = 0;   // kernels of this library launched (the radix sort's are counted apart)
@@ -1250,13 +1279,13 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
     // waits for it before the first kernel that writes bins
     if (!staged) {
         const cudaStream_t side = side_stream_.s;
-        EventTimer mt(timing, side);
+        EventTimer mt(timing, side, &pending_timings_);
         BCSIM_CUDA(cudaEventRecord(ev_fork_.e, st));
         BCSIM_CUDA(cudaStreamWaitEvent(side, ev_fork_.e, 0));
         if (timing) mt.restart();
         BCSIM_CUDA(cudaMemsetAsync(bins, 0, P.bins_bytes, side));
         BCSIM_CUDA(cudaEventRecord(ev_join_.e, side));
-        if (timing) debug_["kernel_memset_ms"].push_back(mt.stop());
+        if (timing) mt.stop("kernel_memset_ms");
     }
     bool joined = staged;
     auto join_bins = [&]() {
@@ -1273,7 +1302,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         const int64_t N = P.n_shared;
         timer.restart();
         if (!staged) enqueue_records(st, &launches);
-        if (timing) debug_["prep_sort_ms"].push_back(timer.stop());
+        if (timing) timer.stop("prep_sort_ms");
         timer.restart();
 
         join_bins();
@@ -1301,7 +1330,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                                   pair_counts, g.threads));
             }
         }
-        if (timing) debug_["fixed_projection_kernel_ms"].push_back(timer.stop());
+        if (timing) timer.stop("fixed_projection_kernel_ms");
     }
 
     // per-pair path
@@ -1327,7 +1356,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
                                                   pair_counts, g.threads));
         }
     }
-    if (timing) debug_[P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms"].push_back(timer.stop());
+    if (timing) timer.stop(P.shared ? "spline_projection_kernel_ms" : "fixed_projection_kernel_ms");
 
     // convolution + demodulation + decimation; with a host destination in
     // blocks of lines, each block's IQ copied out while the next is convolved
@@ -1381,8 +1410,8 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
         if (wait_copies) BCSIM_CUDA(cudaStreamWaitEvent(st, ev_copied_.e, 0));
     }
     if (timing) {
-        debug_["kernel_convolve_demodulate_ms"].push_back(timer.stop());
-        debug_["total_ms"].push_back(total.stop());
+        timer.stop("kernel_convolve_demodulate_ms");
+        total.stop("total_ms");
     }
     last_launches_ = launches;
 }
@@ -1390,6 +1419,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
 void Simulator::simulate(float2* dev_out, float* host_out) {
     prepare();
     if (store_details_) debug_.clear();
+    drop_timings();
     const cudaStream_t st = stream_;
     enqueue(st, dev_out, store_details_, host_out);
     if (count_pairs_ && mode_ == MODE_FP64) {
@@ -1402,14 +1432,17 @@ void Simulator::simulate(float2* dev_out, float* host_out) {
         debug_["per_pair_evaluated_pairs"] = {(double)c[3]};
     }
     if (host_out) {
-        EventTimer timer(store_details_, st);
+        EventTimer timer(store_details_, st, &pending_timings_);
         // (the IQ was copied by enqueue, overlapped with the convolution)
         // the bounded-wait error flag travels with the result (one synchronisation)
         if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
         BCSIM_CUDA(enqueue_error_flag_read(err_flag_dev_.as<int>(), flag_host_.p, st));
+        if (store_details_) timer.stop("kernel_memcpy_ms");
         BCSIM_CUDA(cudaStreamSynchronize(st));
-        if (store_details_) debug_["kernel_memcpy_ms"].push_back(timer.stop());
+        if (store_details_) resolve_timings();
         if (*flag_host_.p) check_device_flag();   // clears the flag and reports
+    } else if (store_details_) {
+        resolve_timings();   // waits for the simulation (timed calls only)
     }
 }
 

@@ -148,6 +148,13 @@ struct RecordSet {
 };
 
 // An event without timing, destroyed with its owner.
+// A stage interval of a timed simulation (store_kernel_details): its start
+// and end events, read after the simulation has finished.
+struct PendingTiming {
+    const char* key;
+    cudaEvent_t a, b;
+};
+
 struct OwnedEvent {
     cudaEvent_t e = nullptr;
     OwnedEvent() = default;
@@ -374,6 +381,9 @@ private:
     std::vector<float> pinned_dummy_;
 
     std::map<std::string, std::vector<double>> debug_;
+    std::vector<PendingTiming> pending_timings_;   // stage intervals recorded, not yet read
+    void resolve_timings();
+    void drop_timings();
     LogFn log_fn_ = nullptr;
     void* log_user_ = nullptr;
 };
