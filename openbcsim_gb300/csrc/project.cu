@@ -420,13 +420,17 @@ __device__ __forceinline__ LineK load_line(const LineGeom* g, const BeamDev& b) 
     return k;
 }
 
-// One CTA: a chunk of `chunk` (<= 1024) consecutive records, sorted by bin,
-// staged once in shared memory by a TMA bulk copy; then the lines, in slots of
-// 32 (one line per lane, in direction order so that a slot's lines point in
-// nearby directions), are handed to the warps one slot at a time as the warps
-// finish the previous one (walk lengths differ between slots), two phases per
-// slot:
-//   A. mask: each lane tests one record against the warp's "slot box": the
+// One CTA: a chunk of `chunk` (<= 1024) consecutive records, sorted by bin
+// (and within a bin by the angular cell of their direction where bins are
+// dense), staged once in shared memory by a TMA bulk copy; then the lines, in
+// slots of 32 (one line per lane, in direction order so that a slot's lines
+// point in nearby directions), are handed to the warps one slot at a time as
+// the warps finish the previous one (walk lengths differ between slots), two
+// phases per slot:
+//   A. mask: where the records carry angular cells, one lane per 32-record
+//      word first tests the word's bounding sphere against the slot box and
+//      whole words are skipped; then each lane tests one record of the words
+//      left against the warp's "slot box": the
 //      lateral/elevational ranges outside which every line of the slot has
 //      weight exactly 0 (the lookup table's extent, or where exp2 underflows),
 //      widened by the spread of the slot's line frames (along the slot's
@@ -705,13 +709,14 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : (THREADS >= 512
         }
 
         // ---- phase B: walk the selected records in order ----
-        // Segment by segment (one FP32 run each), the words of the segment with a
-        // selected record, their bits in order; all of this control is warp-uniform
-        // (segment bounds through redux, words through ballot).  A segment's run is
+        // Segment by segment (one FP32 run each): from the next selected record,
+        // the segment's words with a selected record and their bits in order,
+        // then on to the next selected record past the segment (segments without
+        // one are never visited).  All of this control is warp-uniform (segment
+        // bounds through redux, words through ballot).  A segment's run is
         // folded into the integer total at its end, and at a bin change the total
         // is stored (a plain store inside the chunk, an atomic at its edge bins:
-        // other CTAs hold records there).  Segments without a selected record cost
-        // a few instructions and no fold.
+        // other CTAs hold records there).
         // COUNT: pairs visited, pairs with a non-zero weight, walk steps in which
         // no lane of the warp had a non-zero weight
         unsigned walked = 0, weighted = 0, idle_steps = 0;
