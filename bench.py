@@ -124,6 +124,19 @@ def rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum of this rank's values over the process group (the
+    slowest replica's times), or the values themselves on one rank."""
+    import torch
+
+    dist = torch.distributed
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms while active."""
 
@@ -252,11 +265,7 @@ def run_gpu(args):
             if _has(sim, k):
                 stage.setdefault(k, []).append(sim.get_debug_data(k)[-1])
     sim.set_parameter("store_kernel_details", "off")
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks([sum(step_ms) / 1e3], "cuda")[0]
     projections = job.projections
     value = projections * args.steps * world / total_s
 
@@ -312,10 +321,7 @@ def run_gpu(args):
         t0 = time.perf_counter()
         sim.simulate_fixed_frames([host_in[0]] * args.steps, outs)
         e2e_total = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_total, e2e_single], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total, e2e_single = float(t[0].item()), float(t[1].item())
+    e2e_total, e2e_single = max_over_ranks([e2e_total, e2e_single], "cuda")
     h2d = sum(h.nbytes for h in host_in) + sum(kn.nbytes + cp.nbytes + am.nbytes for _, kn, cp, am in host_sp)
     d2h = L * nd * 8
 
@@ -408,7 +414,7 @@ def run_gpu(args):
         "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
         "wall_s": wall,
     }
-    if not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline:   # the host baseline at N = 1 only
         result["cpu_baseline"] = cpu_baseline(job, args.cpu_seconds)
     if world == 1 and not args.no_extras:
         # the metric's other figures, each outside every timed region above:

@@ -16,6 +16,9 @@
 #include <string>
 #include <vector>
 #include <complex>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdexcept>
 #include "cole_case.h"
 #include "LibBCSim.hpp"
@@ -204,7 +207,16 @@ int ref_scan_convert_u8(const unsigned char* in, int beams, int range, int kind,
 }  // extern "C"
 
 static void configure(bcsim::IAlgorithm* sim, const cole_case* c, int num_threads) {
-        if (num_threads > 0) sim->set_parameter("num_cpu_cores", std::to_string(num_threads));
+        if (num_threads > 0) {
+#ifdef _OPENMP
+            // the reference accepts at most omp_get_max_threads() cores
+            // (CpuAlgorithm.cpp:203-215): raise this thread's OpenMP limit to the
+            // requested count first, as process launchers (torchrun) start their
+            // workers with OMP_NUM_THREADS=1
+            if (num_threads > omp_get_max_threads()) omp_set_num_threads(num_threads);
+#endif
+            sim->set_parameter("num_cpu_cores", std::to_string(num_threads));
+        }
         sim->set_parameter("sound_speed", fstr(c->sound_speed));
         sim->set_parameter("use_arc_projection", c->use_arc_projection ? "on" : "off");
         sim->set_parameter("phase_delay", c->phase_delay ? "on" : "off");
