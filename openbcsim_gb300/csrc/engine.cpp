@@ -1360,11 +1360,12 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
 
     // convolution + demodulation + decimation; with a host destination in
     // blocks of lines, each block's IQ copied out while the next is convolved
+    // (in a stream of frames the copies overlap the next frame instead: one block)
     timer.restart();
     const bool use_fft = convolution_ == 2 || (convolution_ == 0 && fft_ok_ && fft_faster(L, nd_, tap_count_, M_, sms_));
     last_route_fft_ = use_fft;
     route_known_ = true;
-    const int nblocks = (host_out && L >= 1024) ? 4 : 1;
+    const int nblocks = (host_out && L >= 1024 && !staged) ? 4 : 1;
     while ((int)ev_blocks_.size() < nblocks) {
         cudaEvent_t e = nullptr;
         BCSIM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
