@@ -17,9 +17,11 @@ convolution, demodulation, decimation).  Prints one JSON line on rank 0.
 * e2e: the same metric through the C ABI with host buffers, host wall clock:
   every step (frame) uploads the scatterers from pinned host memory and reads
   the IQ back.  A fixed-scatterer phantom runs as a stream of frames through
-  bcsim_simulate_fixed_frames (frame k+1's upload overlaps frame k); splines
-  per step (bcsim_set_*_scatterers + bcsim_simulate_lines).  e2e.single_frame
-  is the per-step form for every workload.
+  bcsim_simulate_fixed_frames, a spline phantom through
+  bcsim_simulate_spline_frames (frame k+1's upload overlaps frame k), where a
+  frame's data exceed L2; otherwise per step (bcsim_set_*_scatterers +
+  bcsim_simulate_lines).  e2e.single_frame is the per-step form for every
+  workload.
 * roofline: the projection kernel against the FP32 pipe: the per-projection
   flop count (flops_per_projection) times the pairs the kernel visits (counted
   by one instrumented run outside the timed region; the exact slot masks skip
@@ -311,15 +313,28 @@ def run_gpu(args):
     bins_bytes = L * job.num_samples * (16 if job.phase_delay else 8)
     l2_bytes = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", 0) or (129 << 20)
     frames_mode = len(host_in) == 1 and not host_sp and bins_bytes > 2 * l2_bytes
+    # a stream of spline frames (bcsim_simulate_spline_frames): every frame
+    # uploads fresh control points and amplitudes, which with its bins exceed
+    # L2 (0.23 GB on the spline sector)
+    sp_bytes = sum(kn.nbytes + cp.nbytes + am.nbytes for _, kn, cp, am in host_sp)
+    spline_frames_mode = not host_in and len(host_sp) == 1 and sp_bytes + bins_bytes > 1.5 * l2_bytes
     e2e_total = e2e_single
-    if frames_mode:
+    if frames_mode or spline_frames_mode:
         outs = [torch.empty((L, nd), dtype=torch.complex64, pin_memory=True).numpy() for _ in range(args.steps)]
         W = max(1, min(args.warmup, args.steps))
-        sim.simulate_fixed_frames([host_in[0]] * W, outs[:W])
+
+        def stream_of(count, o):
+            if frames_mode:
+                sim.simulate_fixed_frames([host_in[0]] * count, o)
+            else:
+                deg, kn, cp, am = host_sp[0]
+                sim.simulate_spline_frames(deg, kn, [cp] * count, [am] * count, o)
+
+        stream_of(W, outs[:W])
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sim.simulate_fixed_frames([host_in[0]] * args.steps, outs)
+        stream_of(args.steps, outs)
         e2e_total = time.perf_counter() - t0
     e2e_total, e2e_single = max_over_ranks([e2e_total, e2e_single], "cuda")
     h2d = sum(h.nbytes for h in host_in) + sum(kn.nbytes + cp.nbytes + am.nbytes for _, kn, cp, am in host_sp)
@@ -385,6 +400,9 @@ def run_gpu(args):
                 "ms_per_step": e2e_total * 1e3 / args.steps,
                 "mode": ("frames: one bcsim_simulate_fixed_frames call of `steps` frames from pinned host memory, "
                          "frame k+1 uploaded while frame k is simulated; one frame's bins exceed L2") if frames_mode else
+                        ("spline frames: one bcsim_simulate_spline_frames call of `steps` frames from pinned host "
+                         "memory, frame k+1's control points uploaded while frame k is simulated; one frame's "
+                         "upload and bins exceed L2") if spline_frames_mode else
                         "per step: clear + add scatterers (upload), simulate_lines (IQ to pinned host memory), L2 flushed",
                 "single_frame": {"value": projections * args.steps * world / e2e_single,
                                  "ms_per_step": e2e_single * 1e3 / args.steps,

@@ -137,6 +137,23 @@ int bcsim_simulate_lines(bcsim_handle* h, float* out, int64_t cap_complex,
 int bcsim_simulate_fixed_frames(bcsim_handle* h, const float* const* xyza_frames, int64_t n, int num_frames,
                                 float* const* iq_out_frames, int64_t cap_complex);
 
+/* A stream of spline frames (beside IAlgorithm: the reference's per-frame
+ * clear_spline_scatterers + add_spline_scatterers + simulate_lines,
+ * LibBCSim.hpp:63-70,81, in one call).  Every frame has the given degree and
+ * knots (num_knots = num_cs + degree + 1); frame k's control points
+ * cps_frames[k] (float [n][num_cs][3]) and amplitudes amps_frames[k] (float
+ * [n]) replace the spline datasets and frame k is simulated into
+ * iq_out_frames[k] (host, cap_complex complex64 values,
+ * [num_lines][num_samples]) -- bit for bit what those three calls per frame
+ * give.  Frame k+1 is uploaded, laid out and its amplitude bound reduced on a
+ * stream of its own while frame k is simulated; pinned host frames let the
+ * copies overlap.  Blocks until every frame's IQ is on the host; the last
+ * frame stays the spline dataset.  An error stops at the failing frame (which
+ * then is the spline dataset). */
+int bcsim_simulate_spline_frames(bcsim_handle* h, int degree, const float* knots, int num_knots,
+                                 const float* const* cps_frames, const float* const* amps_frames, int64_t n,
+                                 int num_cs, int num_frames, float* const* iq_out_frames, int64_t cap_complex);
+
 /* simulate_lines into a device buffer (complex64 [num_lines][num_samples], at
  * least 16-byte aligned) on the handle's stream, without a host copy and
  * without synchronising.  For callers that keep the IQ on the GPU. */

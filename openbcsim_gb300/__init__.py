@@ -189,6 +189,44 @@ class RfSimulator:
         self._check(self._lib.bcsim_simulate_fixed_frames(self._h, fp, n, len(frames), op, L * nd))
         return outs
 
+    def simulate_spline_frames(self, degree, knots, cps_frames, amps_frames, outs=None):
+        """A stream of spline frames of one shape: frame k's control points
+        cps_frames[k] ([n, num_cs, 3] float32) and amplitudes amps_frames[k] ([n]
+        float32), with the given degree and knots, replace the spline datasets;
+        returns (or fills) one IQ array [num_lines, num_samples] complex64 per
+        frame, bit for bit what clear_spline_scatterers + add_spline_scatterers +
+        simulate_lines_line_major per frame give.  The next frame's upload
+        overlaps the current frame's simulation (pinned host arrays let the
+        copies run asynchronously)."""
+        knots = np.ascontiguousarray(knots, np.float32)
+        cps_frames = [np.ascontiguousarray(c) for c in cps_frames]
+        amps_frames = [np.ascontiguousarray(a) for a in amps_frames]
+        if not cps_frames:
+            return []
+        if len(amps_frames) != len(cps_frames):
+            raise ValueError("one amplitude array per frame")
+        shape = cps_frames[0].shape
+        if len(shape) != 3 or shape[2] != 3:
+            raise ValueError("control points must be [n, num_cs, 3] float32 arrays")
+        n, num_cs = shape[0], shape[1]
+        for c, a in zip(cps_frames, amps_frames):
+            if c.dtype != np.float32 or c.shape != shape or a.dtype != np.float32 or a.shape != (n,):
+                raise ValueError("every frame must hold float32 [n, num_cs, 3] control points and [n] amplitudes")
+        L, nd = self.output_shape()
+        if outs is None:
+            outs = [np.empty((L, nd), np.complex64) for _ in cps_frames]
+        if len(outs) != len(cps_frames) or any(o.shape != (L, nd) or o.dtype != np.complex64 or
+                                               not o.flags.c_contiguous for o in outs):
+            raise ValueError("outs must hold one C-contiguous complex64 [num_lines, num_samples] array per frame")
+        f = C.POINTER(C.c_float)
+        cp = (f * len(cps_frames))(*[c.ctypes.data_as(f) for c in cps_frames])
+        ap = (f * len(amps_frames))(*[a.ctypes.data_as(f) for a in amps_frames])
+        op = (f * len(outs))(*[o.ctypes.data_as(f) for o in outs])
+        self._check(self._lib.bcsim_simulate_spline_frames(self._h, int(degree), knots.ctypes.data_as(f),
+                                                           knots.size, cp, ap, n, num_cs, len(cps_frames), op,
+                                                           L * nd))
+        return outs
+
     def simulate_lines_device(self, device_ptr: int, capacity: int):
         """IQ into a device buffer of `capacity` complex64 values (no host copy)."""
         self._check(self._lib.bcsim_simulate_lines_device(self._h, C.c_void_p(device_ptr), int(capacity)))

@@ -40,6 +40,9 @@ SIGNATURES = [
     ("bcsim_simulate_lines", C.c_int, [C.c_void_p, _f32p, C.c_int64, _i64p, _i64p]),
     ("bcsim_simulate_fixed_frames", C.c_int, [C.c_void_p, C.POINTER(_f32p), C.c_int64, C.c_int, C.POINTER(_f32p),
                                               C.c_int64]),
+    ("bcsim_simulate_spline_frames", C.c_int, [C.c_void_p, C.c_int, _f32p, C.c_int, C.POINTER(_f32p),
+                                               C.POINTER(_f32p), C.c_int64, C.c_int, C.c_int, C.POINTER(_f32p),
+                                               C.c_int64]),
     ("bcsim_simulate_lines_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     ("bcsim_get_stream", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("bcsim_get_debug_data", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.c_int64, _i64p]),

@@ -171,6 +171,15 @@ int bcsim_simulate_fixed_frames(bcsim_handle* h, const float* const* xyza_frames
     return guarded(h, [&] { h->sim.simulate_fixed_frames(xyza_frames, n, num_frames, iq_out_frames, cap_complex); });
 }
 
+int bcsim_simulate_spline_frames(bcsim_handle* h, int degree, const float* knots, int num_knots,
+                                 const float* const* cps_frames, const float* const* amps_frames, int64_t n,
+                                 int num_cs, int num_frames, float* const* iq_out_frames, int64_t cap_complex) {
+    return guarded(h, [&] {
+        h->sim.simulate_spline_frames(degree, knots, num_knots, cps_frames, amps_frames, n, num_cs, num_frames,
+                                      iq_out_frames, cap_complex);
+    });
+}
+
 int bcsim_simulate_lines_device(bcsim_handle* h, void* device_out, int64_t cap_complex) {
     return guarded(h, [&] { h->sim.simulate_device(device_out, cap_complex); });
 }

@@ -1241,7 +1241,7 @@ void Simulator::enqueue_records(cudaStream_t st, int* launches) {
         if (!P.spline_shared[d]) continue;
         const SplineDataset& ds = splines_[d];
         ++*launches;
-        BCSIM_CUDA(launch_prep_shared_spline(ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+        BCSIM_CUDA(launch_prep_shared_spline(ds.cps_dev(), ds.amps_dev(), ds.n, ds.num_cs,
                                              P.spline_first_cs[d], ds.degree, spl_basis_d_.as<double>() + 64 * d,
                                              spl_basis_f_.as<float>() + 64 * d, P.spline_off[d], origin, p, b,
                                              R.keys_in.as<uint32_t>(), R.vals_in.as<uint32_t>(), R.recA.as<float4>(),
@@ -1322,7 +1322,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
             } else if (P.spline_shared[g.d]) {
                 const SplineDataset& ds = splines_[g.d];
                 ++launches;
-                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps_dev(), ds.amps_dev(), ds.n, ds.num_cs,
                                                   ds.degree, R.vals_out.as<uint32_t>(), R.counts.as<int>(),
                                                   P.spline_off[g.d], lines_d, gen_line_ids_.as<int>(),
                                                   gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
@@ -1349,7 +1349,7 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
             if (P.spline_shared[g.d]) continue;
             const SplineDataset& ds = splines_[g.d];
             ++launches;
-                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps.as<float4>(), ds.amps.as<float>(), ds.n, ds.num_cs,
+                BCSIM_CUDA(launch_project_generic(nullptr, ds.cps_dev(), ds.amps_dev(), ds.n, ds.num_cs,
                                               ds.degree, nullptr, nullptr, 0, lines_d, gen_line_ids_.as<int>(),
                                               gen_tiles_.as<LineTile>() + g.tile_off, (int)g.num_tiles,
                                               gen_basis_.as<LineBasis>() + g.basis_off, p, b, bins, st, P.tile_cull ? gen_boxes_.as<TileBox>() + g.tile_off : nullptr,
@@ -1360,12 +1360,13 @@ void Simulator::enqueue(cudaStream_t st, float2* dev_out, bool timing, float* ho
 
     // convolution + demodulation + decimation; with a host destination in
     // blocks of lines, each block's IQ copied out while the next is convolved
-    // (in a stream of frames the copies overlap the next frame instead: one block)
+    // (in a stream of frames, wait_copies off, the copies overlap the next frame
+    // instead: one block)
     timer.restart();
     const bool use_fft = convolution_ == 2 || (convolution_ == 0 && fft_ok_ && fft_faster(L, nd_, tap_count_, M_, sms_));
     last_route_fft_ = use_fft;
     route_known_ = true;
-    const int nblocks = (host_out && L >= 1024 && !staged) ? 4 : 1;
+    const int nblocks = (host_out && L >= 1024 && wait_copies) ? 4 : 1;
     while ((int)ev_blocks_.size() < nblocks) {
         cudaEvent_t e = nullptr;
         BCSIM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1644,6 +1645,121 @@ void Simulator::simulate_fixed_frames(const float* const* frames, int64_t n, int
             // last block is still copied to the host
             if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_out_free_[b].e, 0));
             enqueue(stream_, frame_out_[b].as<float2>(), false, outs[k], false, true);
+            BCSIM_CUDA(cudaEventRecord(ev_consumed_[b].e, stream_));
+            BCSIM_CUDA(cudaEventRecord(ev_out_free_[b].e, copy_stream_.s));
+        }
+        BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_copied_.e, 0));   // the last frame's copies
+        if (!flag_host_.p) BCSIM_CUDA(cudaMallocHost(&flag_host_.p, sizeof(int)));
+        BCSIM_CUDA(enqueue_error_flag_read(err_flag_dev_.as<int>(), flag_host_.p, stream_));
+    } catch (...) {
+        settle();
+        throw;
+    }
+    settle();
+    if (*flag_host_.p) check_device_flag();
+}
+
+// The spline counterpart of simulate_fixed_frames: per frame the reference's
+// clear_spline_scatterers + add_spline_scatterers + simulate_lines
+// (LibBCSim.hpp:63-70,81), with frame k+1's control points uploaded, laid out
+// [K][n] and their amplitude bound reduced on the upload stream while frame k
+// is simulated.  The frames share one shape (degree, knots, n, num_cs), so the
+// plan (line bases, tiles, culling boxes) is kept; each frame redoes the
+// fixed-point scale.
+void Simulator::simulate_spline_frames(int degree, const float* knots, int num_knots, const float* const* cps_frames,
+                                       const float* const* amps_frames, int64_t n, int num_cs, int num_frames,
+                                       float* const* outs, int64_t cap_complex) {
+    if (num_frames <= 0) return;
+    if (n <= 0 || num_cs <= 0 || !cps_frames || !amps_frames || !outs || num_knots < 0 || (num_knots > 0 && !knots))
+        throw SimError(BCSIM_E_INVALID, "simulate_spline_frames: invalid data");
+    // src/python/PythonInterface.cpp:150-153, as add_spline_scatterers
+    if (num_knots != num_cs + degree + 1)
+        throw SimError(BCSIM_E_INVALID, "add_spline_scatterers : mismatch in number of nodes, degree and control points");
+    if (degree < 0 || degree > MAX_SPLINE_DEGREE)
+        throw SimError(BCSIM_E_INVALID, "add_spline_scatterers : spline degree must be in [0, " +
+                                            std::to_string(MAX_SPLINE_DEGREE) + "]");
+    for (int k = 0; k < num_frames; k++)
+        if (!cps_frames[k] || !amps_frames[k] || !outs[k])
+            throw SimError(BCSIM_E_INVALID, "simulate_spline_frames: null frame or output");
+    ensure_device();
+    int64_t L = 0, nd = 0;
+    output_shape(&L, &nd);
+    if (cap_complex < L * nd)
+        throw SimError(BCSIM_E_CAPACITY, "output buffer too small: need " + std::to_string(L * nd) + " complex values");
+    const size_t raw_bytes = (size_t)n * num_cs * 3 * sizeof(float);
+    const size_t cps_bytes = (size_t)num_cs * n * sizeof(float4);
+    const size_t amp_bytes = (size_t)n * sizeof(float);
+    for (int b = 0; b < 2; b++) {
+        frame_raw_[b].reserve(raw_bytes, stream_);
+        frame_cps_[b].reserve(cps_bytes, stream_);
+        frame_amps_[b].reserve(amp_bytes, stream_);
+        frame_scratch_[b].reserve(abs_sum_scratch_bytes(), stream_);
+        frame_out_[b].reserve((size_t)L * nd * sizeof(float2), stream_);
+    }
+    if (!frame_bounds_.p) BCSIM_CUDA(cudaMallocHost(&frame_bounds_.p, sizeof(FrameBounds)));
+    BCSIM_CUDA(cudaStreamSynchronize(stream_));   // the buffers exist before the upload stream uses them
+    const cudaStream_t up = upload_stream_.s;
+    // frame k: into buffer k & 1, once the frame that read it last (k - 2) is done
+    auto upload = [&](int k) {
+        const int b = k & 1;
+        if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(up, ev_consumed_[b].e, 0));
+        BCSIM_CUDA(cudaMemcpyAsync(frame_raw_[b].get(), cps_frames[k], raw_bytes, cudaMemcpyHostToDevice, up));
+        BCSIM_CUDA(launch_spline_transpose(frame_raw_[b].as<float>(), n, num_cs, frame_cps_[b].as<float4>(), up));
+        BCSIM_CUDA(cudaMemcpyAsync(frame_amps_[b].get(), amps_frames[k], amp_bytes, cudaMemcpyHostToDevice, up));
+        BCSIM_CUDA(abs_sum_enqueue(frame_amps_[b].as<float>(), 1, n, frame_scratch_[b].get(),
+                                   &frame_bounds_.p->sum[b], &frame_bounds_.p->nonfinite[b], up));
+        BCSIM_CUDA(cudaEventRecord(ev_uploaded_[b].e, up));
+    };
+    // one spline dataset of the frames' shape in place of the spline datasets
+    splines_.clear();
+    {
+        SplineDataset ds;
+        ds.degree = degree;
+        ds.num_cs = num_cs;
+        ds.knots.assign(knots, knots + num_knots);
+        ds.n = n;
+        splines_.push_back(std::move(ds));
+    }
+    // a non-finite amplitude stays reported as after the per-frame calls (only
+    // clearing the fixed datasets resets it)
+    const bool base_nonfinite = amplitude_nonfinite_;
+    cfg_version_++;
+    data_version_++;
+    // afterwards (or on an error) the frame last installed is the spline dataset
+    int installed = -1;
+    auto settle = [&]() {
+        cudaStreamSynchronize(up);
+        cudaStreamSynchronize(copy_stream_.s);
+        cudaStreamSynchronize(side_stream_.s);
+        cudaStreamSynchronize(stream_);
+        SplineDataset& ds = splines_[0];
+        if (installed >= 0) {
+            std::swap(ds.cps, frame_cps_[installed & 1]);
+            std::swap(ds.amps, frame_amps_[installed & 1]);
+        }
+        ds.cps_src = nullptr;
+        ds.amps_src = nullptr;
+        if (installed < 0) splines_.clear();   // nothing was installed: no spline dataset
+    };
+    try {
+        upload(0);
+        for (int k = 0; k < num_frames; k++) {
+            const int b = k & 1;
+            if (k + 1 < num_frames) upload(k + 1);
+            BCSIM_CUDA(cudaEventSynchronize(ev_uploaded_[b].e));   // frame k's amplitude bound
+            SplineDataset& ds = splines_[0];
+            ds.cps_src = frame_cps_[b].as<float4>();
+            ds.amps_src = frame_amps_[b].as<float>();
+            ds.sum_abs_amp = frame_bounds_.p->sum[b];
+            amplitude_nonfinite_ = base_nonfinite || frame_bounds_.p->nonfinite[b] != 0;
+            installed = k;
+            cfg_version_++;
+            data_version_++;
+            prepare();   // a new frame of the same shape: the fixed-point scale
+            BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_uploaded_[b].e, 0));
+            // two device outputs: frame k + 1 runs while frame k's IQ is copied out
+            if (k >= 2) BCSIM_CUDA(cudaStreamWaitEvent(stream_, ev_out_free_[b].e, 0));
+            enqueue(stream_, frame_out_[b].as<float2>(), false, outs[k], false);
             BCSIM_CUDA(cudaEventRecord(ev_consumed_[b].e, stream_));
             BCSIM_CUDA(cudaEventRecord(ev_out_free_[b].e, copy_stream_.s));
         }

@@ -104,6 +104,12 @@ struct SplineDataset {
     DeviceBuffer amps;     // float [n]
     int64_t n = 0;
     double sum_abs_amp = 0.0;
+    // simulate_spline_frames: the current frame's buffers, read in place of the
+    // owned ones while a stream of frames runs (not owned)
+    const float4* cps_src = nullptr;
+    const float* amps_src = nullptr;
+    const float4* cps_dev() const { return cps_src ? cps_src : cps.as<float4>(); }
+    const float* amps_dev() const { return amps_src ? amps_src : amps.as<float>(); }
 };
 
 typedef void (*LogFn)(int level, const char* message, void* user);
@@ -242,6 +248,14 @@ public:
     // double-buffered).  Afterwards the last frame is the fixed dataset.
     void simulate_fixed_frames(const float* const* frames, int64_t n, int num_frames, float* const* outs,
                                int64_t cap_complex);
+    // A stream of spline frames: frame k replaces the spline datasets with one of
+    // the given degree and knots, control points cps_frames[k] ([n][num_cs][3])
+    // and amplitudes amps_frames[k] ([n]), and is simulated into outs[k]; frame
+    // k+1 is uploaded while frame k runs.  Bit for bit clear_spline_scatterers +
+    // add_spline_scatterers + simulate per frame.
+    void simulate_spline_frames(int degree, const float* knots, int num_knots, const float* const* cps_frames,
+                                const float* const* amps_frames, int64_t n, int num_cs, int num_frames,
+                                float* const* outs, int64_t cap_complex);
 
     std::vector<double> get_debug_data(const std::string& key) const;
     void set_logger(LogFn fn, void* user) { log_fn_ = fn; log_user_ = user; }
@@ -341,6 +355,7 @@ private:
     // all fixed datasets, appended into one float4 [n] array (x, y, z, a)
     DeviceBuffer fixed_xyza_;
     DeviceBuffer frame_xyza_[2], frame_scratch_[2], frame_out_[2];   // simulate_fixed_frames' double buffers
+    DeviceBuffer frame_raw_[2], frame_cps_[2], frame_amps_[2];       // simulate_spline_frames' double buffers
     OwnedEvent ev_out_free_[2];   // a frame output buffer's copy to the host done
     PinnedFrameBounds frame_bounds_;
     const float4* fixed_src_ = nullptr;   // the fixed scatterers the kernels read: fixed_xyza_ unless a frame's

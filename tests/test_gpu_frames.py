@@ -94,3 +94,64 @@ def test_frames_argument_errors():
         sim.simulate_fixed_frames([f[0], f[1][:-1]])
     with pytest.raises(RuntimeError):
         sim.simulate_fixed_frames([f[0][:, :3]])
+
+
+def spline_frames_of(sp, count, seed):
+    rng = np.random.default_rng(seed)
+    cps, amps = [], []
+    for _ in range(count):
+        c = sp.control_points + rng.normal(0.0, 2e-4, sp.control_points.shape).astype(np.float32)
+        cps.append(np.ascontiguousarray(c, np.float32))
+        amps.append(np.ascontiguousarray(sp.amplitudes * np.float32(rng.uniform(0.5, 2.0)), np.float32))
+    return cps, amps
+
+
+@pytest.mark.parametrize("shared_time", [False, True])
+def test_spline_frames_equal_per_frame_calls(shared_time):
+    """Streams of spline frames (bcsim_simulate_spline_frames): lines at their
+    own times (the per-pair path) and at one shared time (rendered once into
+    shared-origin records) give, bit for bit, clear_spline_scatterers +
+    add_spline_scatterers + simulate_lines per frame; the last frame stays the
+    spline dataset."""
+    from openbcsim_gb300 import workloads as W
+
+    rng = np.random.default_rng(41)
+    sp = W.random_spline(rng, 30_000, 12)
+    t0, t1 = W.spline_time_limits(sp.degree, sp.knots, 12)
+    ts = np.full(96, 0.5 * (t0 + t1), np.float32) if shared_time else np.linspace(t0, t1, 96).astype(np.float32)
+    scan = W.sector_scan(96, 35.0, 0.12, timestamps=ts)
+    job = W._excitation_job("spline_frames", scan, 2.5e6, 0.1, W.GaussianBeam(1e-3, 1e-3), [], [sp], 10)
+    cps, amps = spline_frames_of(sp, 4, 43)
+    sim = engine(job)
+    outs = sim.simulate_spline_frames(sp.degree, sp.knots, cps, amps)
+    assert len(outs) == len(cps)
+    for k in range(len(cps)):
+        ref = engine(job)
+        ref.clear_spline_scatterers()
+        ref.add_spline_scatterers(sp.degree, sp.knots, cps[k], amps[k])
+        assert np.array_equal(outs[k], ref.simulate_lines_line_major()), k
+    assert not np.array_equal(outs[0], outs[1])
+    assert np.array_equal(sim.simulate_lines_line_major(), outs[-1])
+    assert sim.get_total_num_scatterers() == cps[0].shape[0]
+
+
+def test_spline_frames_stop_at_a_non_finite_amplitude():
+    import openbcsim_gb300 as gb
+    from openbcsim_gb300 import workloads as W
+
+    job = W.sector_spline(num_scatterers=8_000, num_lines=32)
+    sp = job.splines[0]
+    cps, amps = spline_frames_of(sp, 3, 47)
+    amps[1] = amps[1].copy()
+    amps[1][5] = np.nan
+    sim = engine(job)
+    outs = [np.zeros(sim.output_shape(), np.complex64) for _ in cps]
+    with pytest.raises(gb.SimulatorError) as ei:
+        sim.simulate_spline_frames(sp.degree, sp.knots, cps, amps, outs)
+    assert "Nan in scatterer projection." in str(ei.value)
+    ref = engine(job)
+    ref.clear_spline_scatterers()
+    ref.add_spline_scatterers(sp.degree, sp.knots, cps[0], amps[0])
+    assert np.array_equal(outs[0], ref.simulate_lines_line_major())
+    with pytest.raises(ValueError):
+        sim.simulate_spline_frames(sp.degree, sp.knots, cps, amps[:2])
