@@ -42,6 +42,7 @@ Lines are independent, so N GPUs run N independent replicas of the workload
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -659,12 +660,29 @@ def serve_stream(args, phantoms, sims, rate, seconds):
     server, then replayed live by serial plain execution (one simulate_lines
     at a time in arrival order, each starting when the request has arrived and
     the previous one is done).  Latency = arrival to result on the host."""
-    import queue
+    import torch
 
     import openbcsim_gb300 as gb
     from openbcsim_gb300 import workloads as W
 
     reqs = W.request_stream(phantoms, rate_hz=rate, seconds=seconds)
+    # objects of earlier sections that only the cyclic collector frees (their
+    # device teardown synchronises) are freed here, not in the middle of the
+    # stream; the collector stays off while both forms are timed
+    gc.collect()
+    torch.cuda.synchronize()
+    gc.disable()
+    try:
+        return _serve_stream_timed(args, phantoms, sims, rate, seconds, reqs, gb)
+    finally:
+        gc.enable()
+
+
+def _serve_stream_timed(args, phantoms, sims, rate, seconds, reqs, gb):
+    import queue
+
+    from openbcsim_gb300 import workloads as W
+
     server = gb.Server(hbm_budget_bytes=64 << 30, max_slots_per_phantom=4, max_in_flight=args.max_in_flight)
     pids = [server.add_phantom(s) for s in sims]
     # warm-up: per phantom, as many requests of the stream's largest shape (256
