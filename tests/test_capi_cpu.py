@@ -158,3 +158,40 @@ def test_logger_receives_messages(lib):
     s.set_analytical_beam_profile(1e-3, 1e-3)
     assert any("analytical beam profile" in m for _, m in got)
     s.set_logger(None)
+
+
+def test_frame_stream_argument_errors(lib):
+    """bcsim_simulate_fixed_frames / bcsim_simulate_spline_frames check their
+    arguments before any device work: missing data, a knot vector that does not
+    match degree and control points (the reference's message), a degree out of
+    range, null frames; zero frames is a no-op."""
+    h = C.c_void_p()
+    assert lib.bcsim_create(b"gpu", C.byref(h)) == 0
+    f = C.POINTER(C.c_float)
+    knots = np.zeros(8, np.float32)
+    cps = np.zeros((4, 4, 3), np.float32)
+    amps = np.zeros(4, np.float32)
+    out = np.zeros(8, np.complex64)
+    one = lambda a: (f * 1)(a.ctypes.data_as(f))   # noqa: E731
+    kp = knots.ctypes.data_as(f)
+
+    def spline(degree, num_knots, n, num_cs, frames, cps_arr=None, amps_arr=None, out_arr=None):
+        return lib.bcsim_simulate_spline_frames(h, degree, kp, num_knots, cps_arr, amps_arr, n, num_cs, frames,
+                                                out_arr, 8)
+
+    assert spline(3, 8, 4, 4, 0) == 0                                       # no frames: nothing to do
+    assert spline(3, 8, 4, 4, 1) == 1                                       # no frame pointers
+    assert b"simulate_spline_frames: invalid data" in lib.bcsim_last_error(h)
+    assert spline(3, 7, 4, 4, 1, one(cps), one(amps), one(out)) == 1
+    assert b"mismatch in number of nodes, degree and control points" in lib.bcsim_last_error(h)
+    assert spline(9, 14, 4, 4, 1, one(cps), one(amps), one(out)) == 1
+    assert b"spline degree must be in [0, 7]" in lib.bcsim_last_error(h)
+    nulls = (f * 1)()
+    assert spline(3, 8, 4, 4, 1, nulls, one(amps), one(out)) == 1
+    assert b"null frame or output" in lib.bcsim_last_error(h)
+    xyza = np.zeros((4, 4), np.float32)
+    assert lib.bcsim_simulate_fixed_frames(h, one(xyza), 0, 1, one(out), 8) == 1
+    assert b"simulate_fixed_frames: invalid data" in lib.bcsim_last_error(h)
+    assert lib.bcsim_simulate_fixed_frames(h, nulls, 4, 1, one(out), 8) == 1
+    assert b"null frame or output" in lib.bcsim_last_error(h)
+    assert lib.bcsim_destroy(h) == 0
